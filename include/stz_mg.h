@@ -1,0 +1,137 @@
+/* stz_mg -- GB300 multigrid for the quasi-static projection solve.
+ *
+ * C-ABI drop-in for the reference's templated multigrid (nmboffi/stzpp,
+ * mg_3d_template) instantiated as multigrid<vec3, M> with M = mat3 or
+ * sym_mat3.  The reference's interface is a compile-time duck-typed contract;
+ * each entry point below names the member it replaces (paths relative to the
+ * reference checkout).  Plain pointers and sizes only; no CUDA or torch types.
+ *
+ * Data layout at this boundary is the reference's: nodes in natural order
+ * (x fastest, index i + m*(j + n*k)), vec3 fields as 3 consecutive doubles
+ * per node (region::r0 / x0 without ghosts, region.hh:75-83), 3x3 blocks as 9
+ * doubles row-major (mat3, mg_3d_template/mat3.hh), a node's 27 blocks in the
+ * stencil order b = (dx+1) + 3(dy+1) + 9(dz+1) of shear_sim_3d.cpp:224.
+ *
+ * Every function returns STZ_MG_OK (0) or an error code; the message of the
+ * last error on the calling thread is stz_mg_last_error().  The reference
+ * aborts the MPI job instead (p_fatal_error, common.cc:52).  A handle is not
+ * thread safe; all work of a handle runs on its CUDA stream.
+ */
+#ifndef STZ_MG_H
+#define STZ_MG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    STZ_MG_OK = 0,
+    STZ_MG_ERR_ARG = 1,         /* bad argument or call order */
+    STZ_MG_ERR_CUDA = 2,        /* CUDA runtime failure */
+    STZ_MG_ERR_UNSUPPORTED = 3, /* grid shape the GPU path does not support */
+    STZ_MG_ERR_NOCONV = 4,      /* max_cycles reached above tolerance */
+    STZ_MG_ERR_SINGULAR = 5,    /* singular diagonal block or bottom matrix */
+    STZ_MG_ERR_NONFINITE = 6,   /* NaN/Inf in inputs or iterates */
+    STZ_MG_ERR_OOM = 7          /* device allocation failed */
+};
+
+enum { STZ_MG_FP64 = 0, STZ_MG_MIXED = 1 };          /* precision */
+enum { STZ_MG_BOTTOM_DIRECT = 0, STZ_MG_BOTTOM_GS = 1 };
+enum { STZ_MG_HOST = 0, STZ_MG_DEVICE = 1 };        /* where a pointer lives */
+enum { STZ_MG_FIELD_X = 0, STZ_MG_FIELD_R = 1 };
+
+typedef struct stz_mg_handle_s *stz_mg_handle;
+
+/* Problem and solver description.  m, n, o and the periodicity replace the
+ * geometry / sim fields the region ctor reads (region.hh:663-700, 792-830):
+ * a periodic dimension with N cells has N nodes, a non-periodic one N+1. */
+typedef struct {
+    int m, n, o;
+    int x_prd, y_prd, z_prd;
+    int precision;      /* STZ_MG_FP64 or STZ_MG_MIXED (FP32 cycles inside FP64 defect correction) */
+    int v_down, v_up;   /* sweeps per level: v_down+i down, v_up+i-1 up (multigrid.hh:123, multigrid.cc:265,288) */
+    int max_coarse;     /* coarsen while the coarsest level has more nodes (reference: 1024, multigrid.cc:40) */
+    int bottom;         /* STZ_MG_BOTTOM_DIRECT (FP64 dense solve) or STZ_MG_BOTTOM_GS */
+    int bottom_sweeps;  /* sweeps of the GS bottom solve (reference: 24, common.hh:57) */
+    int device;         /* CUDA device ordinal */
+    void *stream;       /* cudaStream_t to run on, or NULL for a handle-owned stream */
+} stz_mg_desc;
+
+/* Defaults: FP64, v_down = v_up = 2, max_coarse = 16 (coarsest level of a few
+ * nodes, e.g. 2x2x3), direct bottom, 24 bottom sweeps, device 0, own stream. */
+void stz_mg_desc_default(stz_mg_desc *d);
+
+const char *stz_mg_last_error(void);
+
+/* multigrid(sim, comm_buffer) / multigrid(pr, gm, com) (multigrid.hh:126-189):
+ * builds the level hierarchy (setup_hierarchy, multigrid.cc:19-132). */
+int stz_mg_create(const stz_mg_desc *desc, stz_mg_handle *out);
+int stz_mg_destroy(stz_mg_handle h);
+
+/* Shared stencil of interior nodes and `fix` block of Dirichlet nodes: the
+ * external_ptr path (shear_sim_3d.hh:388-402; stencil/fix set up by
+ * set_up_stencil_and_matrices, shear_sim_3d.hh:45-55).  27*9 and 9 doubles. */
+int stz_mg_set_stencil_const(stz_mg_handle h, const double *stencil, const double *fix);
+
+/* Per-node stencils, npts*27*9 doubles (a Dirichlet node uses block 13 only):
+ * the internal()/mem_size()/fill_entries() path (region.hh:196-206). */
+int stz_mg_set_stencil_points(stz_mg_handle h, const double *A, int where);
+
+/* Variable-coefficient operator -dt*div(mu(grad u + grad u^T) + lam div(u) I)
+ * from per-node mu, lambda (npts doubles each), applied matrix-free on the
+ * top level.  With constant mu, lambda it is the stencil of
+ * shear_sim_3d::set_up_stencil_base (shear_sim_3d.cpp:215-331). */
+int stz_mg_set_coeffs_lame(stz_mg_handle h, const double *mu, const double *lam, double dx, double dy,
+                           double dz, double dt, int where);
+
+/* multigrid::setup_matrices -> compute_rats (multigrid.hh:194-198,
+ * multigrid.cc:330-344): Galerkin coarse operators on every level.  Call again
+ * after a coefficient change. */
+int stz_mg_setup(stz_mg_handle h);
+
+/* multigrid::setup_fields (region.hh:209-241): right-hand side and initial
+ * guess, 3*npts doubles. */
+int stz_mg_set_rhs(stz_mg_handle h, const double *r, int where);
+int stz_mg_set_x(stz_mg_handle h, const double *x, int where);
+/* The solution, read by the drivers through reg[0]->x0 (shear_sim_3d.cpp:616-674). */
+int stz_mg_get_x(stz_mg_handle h, double *x, int where);
+
+/* multigrid::v_cycle (multigrid.cc:253-297).  In mixed precision one call is
+ * one defect-correction step: FP64 residual, one FP32 V-cycle, FP64 update. */
+int stz_mg_vcycle(stz_mg_handle h);
+
+/* V-cycles until |b - A x|_2 <= rel_tol |b|_2 (the loop of
+ * shear_sim_3d::projection_step, shear_sim_3d.cpp:567-582, with the true
+ * residual norm).  cycles = V-cycles run, relres = final relative residual;
+ * STZ_MG_ERR_NOCONV when max_cycles is reached first. */
+int stz_mg_solve(stz_mg_handle h, double rel_tol, int max_cycles, int *cycles, double *relres);
+
+/* |b - A x|_2 and |b|_2 in FP64 on the top level. */
+int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm);
+
+/* region::l2_error_all (region.cc:3030-3057) as shipped: for V = vec3 the
+ * reference sums |r|^4 (its mg3d_mod_sq squares the vec3 -> double cast). */
+int stz_mg_l2_error_all(stz_mg_handle h, double *out);
+
+/* Level-wise operations on the FP64 hierarchy, the region members the
+ * reference's multigrid class calls (used for parity checks). */
+int stz_mg_num_levels(stz_mg_handle h, int *nlevels);
+int stz_mg_level_dims(stz_mg_handle h, int level, int *dims3);
+/* Coefficients as npts*27*9 doubles (zero outside each node's box) and box
+ * bounds S as npts*6 ints (region::S, region.hh:337-344); either may be NULL. */
+int stz_mg_level_operator(stz_mg_handle h, int level, double *A, int *S);
+int stz_mg_level_set_field(stz_mg_handle h, int level, int which, const double *v, int where);
+int stz_mg_level_get_field(stz_mg_handle h, int level, int which, double *v, int where);
+/* region::gauss_seidel (region.cc:1557), 8-colour order */
+int stz_mg_level_gauss_seidel(stz_mg_handle h, int level, int sweeps);
+/* multigrid::restriction(level) (multigrid.cc:436-449): coarse r from the residual of level-1, coarse x = 0 */
+int stz_mg_level_restriction(stz_mg_handle h, int level);
+/* multigrid::interpolation(level) (multigrid.cc:418-430): x(level-1) += P x(level) */
+int stz_mg_level_interpolation(stz_mg_handle h, int level);
+/* region::residual (region.cc:1008) of every node, 3*npts doubles (may be NULL), and sum |r|^2 */
+int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq, int where);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1003 @@
+// Host runtime and C-ABI of the GB300 multigrid (include/stz_mg.h).
+//
+// One handle = one problem on one GPU: the level hierarchy
+// (multigrid::setup_hierarchy, mg_3d_template/multigrid.cc:19-132), the FP64
+// operators of every level (top level as given, coarse levels by RAT), the
+// FP32 copy of the hierarchy used by the mixed-precision solver, the FP64
+// dense inverse of the coarsest level, and the V-cycle (multigrid.cc:253-297)
+// captured once into a CUDA graph per precision and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/stz_mg.h"
+#include "launch.h"
+#include "ops.cuh"
+
+using namespace stzmg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+struct CudaError {
+    int code;
+};
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            set_error(e_ == cudaErrorMemoryAllocation ? STZ_MG_ERR_OOM : STZ_MG_ERR_CUDA,        \
+                      "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);      \
+            throw CudaError{e_ == cudaErrorMemoryAllocation ? STZ_MG_ERR_OOM : STZ_MG_ERR_CUDA}; \
+        }                                                                                        \
+    } while (0)
+
+struct ApiError {
+    int code;
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    throw ApiError{code};
+}
+
+template <typename T>
+struct Level {
+    T *x = nullptr, *r = nullptr, *res = nullptr;   // 3*npad each
+    T *coef = nullptr, *dinv = nullptr;             // dense levels
+};
+
+constexpr int kMaxLev = 16;
+
+}  // namespace
+
+struct stz_mg_handle_s {
+    stz_mg_desc d;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    int nlev = 0;
+    Geom geo[kMaxLev];
+    Level<double> L64[kMaxLev];
+    Level<float> L32[kMaxLev];
+    LevelOp<double> op64[kMaxLev];
+    LevelOp<float> op32[kMaxLev];
+    int *S[kMaxLev] = {};
+    int top_kind = -1;          // OpKind of the top level once set
+    double *mu64 = nullptr, *lam64 = nullptr;
+    float *mu32 = nullptr, *lam32 = nullptr;
+    double *top_coef64 = nullptr, *top_dinv64 = nullptr;  // per-point top level
+    float *top_coef32 = nullptr, *top_dinv32 = nullptr;
+    // bottom
+    double *ainv_t = nullptr;
+    int *nat_slot = nullptr;
+    int nbot_rows = 0;
+    // scratch
+    double *partial = nullptr;
+    int partial_len = 0;
+    double *dscal = nullptr;    // device scalars
+    double *hscal = nullptr;    // pinned host scalars
+    int *dflag = nullptr;
+    double *stage = nullptr;    // device staging for host<->device natural-order copies
+    size_t stage_len = 0;
+    double bnorm = -1.0;
+    bool setup_done = false;
+    cudaGraphExec_t gx64 = nullptr, gx32 = nullptr;
+    std::vector<void *> allocs;
+
+    template <typename T>
+    T *alloc(size_t n) {
+        void *p = nullptr;
+        CK(cudaMalloc(&p, n * sizeof(T) ? n * sizeof(T) : 1));
+        allocs.push_back(p);
+        return (T *)p;
+    }
+    void release(void *p) {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p);
+        if (it != allocs.end()) {
+            cudaFree(p);
+            allocs.erase(it);
+        }
+    }
+};
+
+namespace {
+
+template <typename F>
+int guarded(stz_mg_handle h, F &&f) {
+    try {
+        if (h) CK(cudaSetDevice(h->d.device));
+        f();
+        return STZ_MG_OK;
+    } catch (const ApiError &e) {
+        return e.code;
+    } catch (const CudaError &e) {
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        return set_error(STZ_MG_ERR_OOM, "host allocation failed");
+    }
+}
+
+size_t npts(const Geom &g) { return (size_t)g.m * g.n * g.o; }
+
+void check_launch() { CK(cudaGetLastError()); }
+
+void sync(stz_mg_handle h) {
+    CK(cudaStreamSynchronize(h->st));
+    check_launch();
+}
+
+double *staging(stz_mg_handle h, size_t n) {
+    if (h->stage_len < n) {
+        h->release(h->stage);
+        h->stage = h->alloc<double>(n);
+        h->stage_len = n;
+    }
+    return h->stage;
+}
+
+// Copies a natural-order host or device array of n doubles to device memory.
+const double *to_device(stz_mg_handle h, const double *src, size_t n, int where) {
+    if (!src) fail(STZ_MG_ERR_ARG, "null input pointer");
+    if (where == STZ_MG_DEVICE) return src;
+    if (where != STZ_MG_HOST) fail(STZ_MG_ERR_ARG, "where must be STZ_MG_HOST or STZ_MG_DEVICE");
+    double *d = staging(h, n);
+    CK(cudaMemcpyAsync(d, src, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    return d;
+}
+
+void need_setup(stz_mg_handle h) {
+    if (!h->setup_done) fail(STZ_MG_ERR_ARG, "stz_mg_setup has not been called");
+}
+
+void check_level(stz_mg_handle h, int l) {
+    if (l < 0 || l >= h->nlev) fail(STZ_MG_ERR_ARG, "level %d out of range [0,%d)", l, h->nlev);
+}
+
+// ------------------------------------------------------------ hierarchy
+void build_geometry(stz_mg_handle h) {
+    const stz_mg_desc &d = h->d;
+    h->geo[0] = make_geom(d.m, d.n, d.o, d.x_prd, d.y_prd, d.z_prd);
+    h->nlev = 1;
+    while (npts(h->geo[h->nlev - 1]) > (size_t)d.max_coarse) {
+        const Geom &P = h->geo[h->nlev - 1];
+        int mc = (P.m + (P.xp ? 1 : 2)) >> 1, nc = (P.n + (P.yp ? 1 : 2)) >> 1, oc = (P.o + (P.zp ? 1 : 2)) >> 1;
+        if (mc == P.m && nc == P.n && oc == P.o) break;
+        if (h->nlev == kMaxLev) fail(STZ_MG_ERR_UNSUPPORTED, "more than %d levels", kMaxLev);
+        h->geo[h->nlev++] = make_geom(mc, nc, oc, P.xp, P.yp, P.zp);
+    }
+    // The 8-colour smoother needs every periodic dimension even (or 1): an odd
+    // periodic dimension would couple two nodes of the same colour.
+    for (int l = 0; l < h->nlev; l++) {
+        const Geom &g = h->geo[l];
+        if ((g.xp && g.m > 1 && (g.m & 1)) || (g.yp && g.n > 1 && (g.n & 1)) || (g.zp && g.o > 1 && (g.o & 1)))
+            fail(STZ_MG_ERR_UNSUPPORTED,
+                 "level %d has an odd periodic dimension (%dx%dx%d); the 8-colour smoother needs even periodic sizes",
+                 l, g.m, g.n, g.o);
+        if ((size_t)g.npad * 243 > (size_t)1 << 40) fail(STZ_MG_ERR_UNSUPPORTED, "grid too large");
+    }
+}
+
+void alloc_fields(stz_mg_handle h) {
+    for (int l = 0; l < h->nlev; l++) {
+        const size_t n3 = 3 * (size_t)h->geo[l].npad;
+        Level<double> &A = h->L64[l];
+        A.x = h->alloc<double>(n3);
+        A.r = h->alloc<double>(n3);
+        A.res = h->alloc<double>(n3);
+        CK(cudaMemsetAsync(A.x, 0, n3 * sizeof(double), h->st));
+        CK(cudaMemsetAsync(A.r, 0, n3 * sizeof(double), h->st));
+        CK(cudaMemsetAsync(A.res, 0, n3 * sizeof(double), h->st));
+        h->S[l] = h->alloc<int>(6 * (size_t)h->geo[l].npad);
+        if (h->d.precision == STZ_MG_MIXED) {
+            Level<float> &B = h->L32[l];
+            B.x = h->alloc<float>(n3);
+            B.r = h->alloc<float>(n3);
+            B.res = h->alloc<float>(n3);
+            CK(cudaMemsetAsync(B.x, 0, n3 * sizeof(float), h->st));
+            CK(cudaMemsetAsync(B.r, 0, n3 * sizeof(float), h->st));
+            CK(cudaMemsetAsync(B.res, 0, n3 * sizeof(float), h->st));
+        }
+    }
+    h->partial_len = residual_blocks(h->geo[0]);
+    h->partial = h->alloc<double>(h->partial_len);
+    h->dscal = h->alloc<double>(8);
+    h->dflag = h->alloc<int>(4);
+    CK(cudaMallocHost(&h->hscal, 8 * sizeof(double)));
+}
+
+void release_graphs(stz_mg_handle h) {
+    if (h->gx64) cudaGraphExecDestroy(h->gx64);
+    if (h->gx32) cudaGraphExecDestroy(h->gx32);
+    h->gx64 = h->gx32 = nullptr;
+}
+
+void invalidate(stz_mg_handle h) {
+    h->setup_done = false;
+    release_graphs(h);
+}
+
+// ------------------------------------------------------------ operators
+void set_const_op(stz_mg_handle h, const double *stencil, const double *fix) {
+    ConstOp<double> c{};
+    std::memcpy(c.a, stencil, sizeof(c.a));
+    std::memcpy(c.fix, fix, sizeof(c.fix));
+    bool ok = inverse3(c.a[13], c.inv_int) & inverse3(c.fix, c.inv_fix);
+    if (!ok) fail(STZ_MG_ERR_SINGULAR, "singular centre or fix block");
+    for (int v = 0; v < 243; v++)
+        if (!std::isfinite(stencil[v])) fail(STZ_MG_ERR_NONFINITE, "non-finite stencil entry %d", v);
+    int elastic = 1;
+    for (int b = 0; b < 27; b++)
+        for (int e = 0; e < 9; e++)
+            if (!elastic_entry(b, e) && c.a[b][e] != 0.0) elastic = 0;
+    c.elastic = elastic;
+    ConstOp<float> f{};
+    for (int b = 0; b < 27; b++)
+        for (int e = 0; e < 9; e++) f.a[b][e] = (float)c.a[b][e];
+    for (int e = 0; e < 9; e++) {
+        f.fix[e] = (float)c.fix[e];
+        f.inv_int[e] = (float)c.inv_int[e];
+        f.inv_fix[e] = (float)c.inv_fix[e];
+    }
+    f.elastic = elastic;
+    h->op64[0] = LevelOp<double>{};
+    h->op64[0].kind = OP_CONST;
+    h->op64[0].cop = c;
+    h->op32[0] = LevelOp<float>{};
+    h->op32[0].kind = OP_CONST;
+    h->op32[0].cop = f;
+    h->top_kind = OP_CONST;
+}
+
+}  // namespace
+
+namespace stzmg {
+__global__ void finite_check_kernel(const double *__restrict__ v, size_t n, int *bad) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; t < n; t += (size_t)gridDim.x * blockDim.x)
+        if (!(v[t] - v[t] == 0.0)) { atomicExch(bad, 1); return; }
+}
+}  // namespace stzmg
+
+namespace {
+
+void require_finite(stz_mg_handle h, const double *d, size_t n, const char *what) {
+    CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+    size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 16);
+    finite_check_kernel<<<(unsigned)std::max<size_t>(blocks, 1), 256, 0, h->st>>>(d, n, h->dflag);
+    check_launch();
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    sync(h);
+    if (bad) fail(STZ_MG_ERR_NONFINITE, "%s contains NaN or Inf", what);
+}
+
+// ------------------------------------------------------------ setup
+void build_bottom(stz_mg_handle h) {
+    const int lb = h->nlev - 1;
+    const Geom &g = h->geo[lb];
+    const size_t N = npts(g);
+    if (N > 4096) fail(STZ_MG_ERR_UNSUPPORTED, "direct bottom solve limited to 4096 nodes (have %zu)", N);
+    const int nr = (int)(3 * N);
+    // dense operator of the bottom level, natural order
+    std::vector<double> Anat(243 * N);
+    {
+        double *dcoef = nullptr;
+        const double *src = nullptr;
+        if (lb == 0 && h->top_kind != OP_DENSE) {
+            dcoef = h->alloc<double>(243 * (size_t)g.npad);
+            launch_expand_dense(h->op64[0], g, dcoef, h->st);
+            src = dcoef;
+        } else {
+            src = lb == 0 ? h->top_coef64 : h->L64[lb].coef;
+        }
+        double *nat = staging(h, 243 * N);
+        launch_coef_cb_to_nat(g, src, nat, h->st);
+        check_launch();
+        CK(cudaMemcpyAsync(Anat.data(), nat, 243 * N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        h->release(dcoef);
+    }
+    std::vector<int> Snat(6 * N);
+    {
+        int *tmp = h->alloc<int>(6 * N);
+        launch_bounds_cb_to_nat(g, h->S[lb], tmp, h->st);
+        check_launch();
+        CK(cudaMemcpyAsync(Snat.data(), tmp, 6 * N * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        h->release(tmp);
+    }
+    std::vector<double> M((size_t)nr * nr, 0.0);
+    auto wrap = [](int a, int len) { a %= len; return a < 0 ? a + len : a; };
+    for (int k = 0; k < g.o; k++)
+        for (int j = 0; j < g.n; j++)
+            for (int i = 0; i < g.m; i++) {
+                size_t p = i + (size_t)g.m * (j + (size_t)g.n * k);
+                const int *S = &Snat[6 * p];
+                for (int dk = S[4]; dk < S[5]; dk++)
+                    for (int dj = S[2]; dj < S[3]; dj++)
+                        for (int di = S[0]; di < S[1]; di++) {
+                            if (di < -1 || di > 1 || dj < -1 || dj > 1 || dk < -1 || dk > 1)
+                                fail(STZ_MG_ERR_UNSUPPORTED, "bottom stencil reaches beyond one node");
+                            int ii = i + di, jj = j + dj, kk = k + dk;
+                            if (g.xp) ii = wrap(ii, g.m);
+                            if (g.yp) jj = wrap(jj, g.n);
+                            if (g.zp) kk = wrap(kk, g.o);
+                            if (ii < 0 || ii >= g.m || jj < 0 || jj >= g.n || kk < 0 || kk >= g.o) continue;
+                            size_t q = ii + (size_t)g.m * (jj + (size_t)g.n * kk);
+                            const double *blk = &Anat[243 * p + 9 * ((di + 1) + 3 * (dj + 1) + 9 * (dk + 1))];
+                            for (int a = 0; a < 3; a++)
+                                for (int c = 0; c < 3; c++) M[(3 * p + a) * nr + 3 * q + c] += blk[3 * a + c];
+                        }
+            }
+    // Gauss-Jordan inverse with partial pivoting, FP64.
+    std::vector<double> inv((size_t)nr * nr, 0.0);
+    for (int i = 0; i < nr; i++) inv[(size_t)i * nr + i] = 1.0;
+    for (int c = 0; c < nr; c++) {
+        int pv = c;
+        double best = std::fabs(M[(size_t)c * nr + c]);
+        for (int r = c + 1; r < nr; r++)
+            if (std::fabs(M[(size_t)r * nr + c]) > best) { best = std::fabs(M[(size_t)r * nr + c]); pv = r; }
+        if (!(best > 0) || !std::isfinite(best)) fail(STZ_MG_ERR_SINGULAR, "bottom-level matrix is singular");
+        if (pv != c)
+            for (int q = 0; q < nr; q++) {
+                std::swap(M[(size_t)c * nr + q], M[(size_t)pv * nr + q]);
+                std::swap(inv[(size_t)c * nr + q], inv[(size_t)pv * nr + q]);
+            }
+        const double piv = 1.0 / M[(size_t)c * nr + c];
+        for (int q = 0; q < nr; q++) { M[(size_t)c * nr + q] *= piv; inv[(size_t)c * nr + q] *= piv; }
+        for (int r = 0; r < nr; r++) {
+            if (r == c) continue;
+            const double f = M[(size_t)r * nr + c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < nr; q++) {
+                M[(size_t)r * nr + q] -= f * M[(size_t)c * nr + q];
+                inv[(size_t)r * nr + q] -= f * inv[(size_t)c * nr + q];
+            }
+        }
+    }
+    std::vector<double> invT((size_t)nr * nr);
+    for (int r = 0; r < nr; r++)
+        for (int c = 0; c < nr; c++) invT[(size_t)c * nr + r] = inv[(size_t)r * nr + c];
+    std::vector<int> ns(N);
+    for (int k = 0; k < g.o; k++)
+        for (int j = 0; j < g.n; j++)
+            for (int i = 0; i < g.m; i++) ns[i + (size_t)g.m * (j + (size_t)g.n * k)] = slot(g, i, j, k);
+    h->release(h->ainv_t);
+    h->release(h->nat_slot);
+    h->ainv_t = h->alloc<double>((size_t)nr * nr);
+    h->nat_slot = h->alloc<int>(N);
+    CK(cudaMemcpyAsync(h->ainv_t, invT.data(), invT.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->nat_slot, ns.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    sync(h);
+    h->nbot_rows = nr;
+}
+
+void setup(stz_mg_handle h) {
+    if (h->top_kind < 0) fail(STZ_MG_ERR_ARG, "no operator: call stz_mg_set_stencil_const, _points or _coeffs_lame first");
+    invalidate(h);
+    const bool mixed = h->d.precision == STZ_MG_MIXED;
+    // top level: dense per-point operator needs its centre inverses
+    if (h->top_kind == OP_DENSE) {
+        const Geom &g = h->geo[0];
+        CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+        launch_dense_dinv<double>(g, h->top_coef64, h->top_dinv64, h->dflag, h->st);
+        check_launch();
+        h->op64[0].dop.dinv = h->top_dinv64;
+        if (mixed) {
+            launch_convert(h->top_coef64, h->top_coef32, 243 * (size_t)g.npad, h->st);
+            launch_convert(h->top_dinv64, h->top_dinv32, 9 * (size_t)g.npad, h->st);
+            check_launch();
+            h->op32[0].dop.coef = h->top_coef32;
+            h->op32[0].dop.dinv = h->top_dinv32;
+        }
+    }
+    launch_top_bounds(h->geo[0], h->S[0], h->st);
+    check_launch();
+    CK(cudaMemsetAsync(h->dflag, 0, 2 * sizeof(int), h->st));
+    for (int l = 1; l < h->nlev; l++) {
+        const Geom &gf = h->geo[l - 1], &gc = h->geo[l];
+        Level<double> &C = h->L64[l];
+        if (!C.coef) {
+            C.coef = h->alloc<double>(243 * (size_t)gc.npad);
+            C.dinv = h->alloc<double>(9 * (size_t)gc.npad);
+        }
+        launch_rat_bounds(gf, h->S[l - 1], gc, h->S[l], h->dflag + 1, h->st);
+        launch_rat(h->op64[l - 1], gf, gc, C.coef, h->st);
+        launch_dense_dinv<double>(gc, C.coef, C.dinv, h->dflag, h->st);
+        check_launch();
+        h->op64[l] = LevelOp<double>{};
+        h->op64[l].kind = OP_DENSE;
+        h->op64[l].dop.coef = C.coef;
+        h->op64[l].dop.dinv = C.dinv;
+        if (mixed) {
+            Level<float> &F = h->L32[l];
+            if (!F.coef) {
+                F.coef = h->alloc<float>(243 * (size_t)gc.npad);
+                F.dinv = h->alloc<float>(9 * (size_t)gc.npad);
+            }
+            launch_convert(C.coef, F.coef, 243 * (size_t)gc.npad, h->st);
+            launch_convert(C.dinv, F.dinv, 9 * (size_t)gc.npad, h->st);
+            check_launch();
+            h->op32[l] = LevelOp<float>{};
+            h->op32[l].kind = OP_DENSE;
+            h->op32[l].dop.coef = F.coef;
+            h->op32[l].dop.dinv = F.dinv;
+        }
+    }
+    int flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(flags, h->dflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    sync(h);
+    if (flags[1]) fail(STZ_MG_ERR_UNSUPPORTED, "RAT box bounds out of range");
+    if (flags[0]) fail(STZ_MG_ERR_SINGULAR, "singular or non-finite diagonal block on a coarse level");
+    if (h->d.bottom == STZ_MG_BOTTOM_DIRECT) build_bottom(h);
+    h->setup_done = true;
+}
+
+// ------------------------------------------------------------ cycles
+template <typename T>
+struct Hier {
+    Level<T> *L;
+    LevelOp<T> *op;
+};
+
+template <typename T>
+void bottom_solve(stz_mg_handle h, Hier<T> H) {
+    const int lb = h->nlev - 1;
+    const Geom &g = h->geo[lb];
+    if (h->d.bottom == STZ_MG_BOTTOM_DIRECT) {
+        launch_bottom_direct<T>(h->nbot_rows, h->ainv_t, h->nat_slot, g.npad, H.L[lb].r, H.L[lb].x, h->st);
+    } else {
+        for (int s = 0; s < h->d.bottom_sweeps; s++) launch_gs_sweep<T>(H.op[lb], g, H.L[lb].r, H.L[lb].x, h->st);
+    }
+}
+
+// multigrid::v_cycle (multigrid.cc:253-297): level i gets v_down+i sweeps
+// going down, then restriction (residual + (1/8)P^T, coarse x cleared); the
+// bottom is solved; going up, interpolation then v_up+i-1 sweeps.
+template <typename T>
+void enqueue_vcycle(stz_mg_handle h, Hier<T> H) {
+    const int L = h->nlev;
+    for (int i = 0; i < L - 1; i++) {
+        const Geom &g = h->geo[i];
+        for (int s = 0; s < h->d.v_down + i; s++) launch_gs_sweep<T>(H.op[i], g, H.L[i].r, H.L[i].x, h->st);
+        launch_residual<T, T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, nullptr, nullptr, h->st);
+        launch_restriction<T>(g, h->geo[i + 1], H.L[i].res, H.L[i + 1].r, h->st);
+        CK(cudaMemsetAsync(H.L[i + 1].x, 0, 3 * (size_t)h->geo[i + 1].npad * sizeof(T), h->st));
+    }
+    bottom_solve<T>(h, H);
+    for (int i = L - 1; i > 0; i--) {
+        launch_interpolation<T>(h->geo[i - 1], h->geo[i], H.L[i].x, H.L[i - 1].x, h->st);
+        for (int s = 0; s < h->d.v_up + i - 1; s++)
+            launch_gs_sweep<T>(H.op[i - 1], h->geo[i - 1], H.L[i - 1].r, H.L[i - 1].x, h->st);
+    }
+}
+
+template <typename T>
+cudaGraphExec_t capture_vcycle(stz_mg_handle h, Hier<T> H) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue_vcycle<T>(h, H);
+    } catch (...) {
+        cudaStreamEndCapture(h->st, &graph);
+        throw;
+    }
+    CK(cudaStreamEndCapture(h->st, &graph));
+    cudaGraphExec_t ex;
+    CK(cudaGraphInstantiate(&ex, graph, 0));
+    CK(cudaGraphDestroy(graph));
+    return ex;
+}
+
+Hier<double> hier64(stz_mg_handle h) { return Hier<double>{h->L64, h->op64}; }
+Hier<float> hier32(stz_mg_handle h) { return Hier<float>{h->L32, h->op32}; }
+
+void run_vcycle64(stz_mg_handle h, int count) {
+    if (!h->gx64) h->gx64 = capture_vcycle<double>(h, hier64(h));
+    for (int c = 0; c < count; c++) CK(cudaGraphLaunch(h->gx64, h->st));
+}
+
+void run_vcycle32(stz_mg_handle h, int count) {
+    if (!h->gx32) h->gx32 = capture_vcycle<float>(h, hier32(h));
+    for (int c = 0; c < count; c++) CK(cudaGraphLaunch(h->gx32, h->st));
+}
+
+// |b - A x|^2 of the top FP64 level; when r32 is non-null the residual is
+// also written there in FP32 (the right-hand side of the correction solve).
+double top_residual_sq(stz_mg_handle h, float *r32) {
+    const Geom &g = h->geo[0];
+    if (r32)
+        launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, r32, h->partial, h->dscal, h->st);
+    else
+        launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial,
+                                        h->dscal, h->st);
+    check_launch();
+    CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    sync(h);
+    double v = h->hscal[0];
+    if (!std::isfinite(v)) fail(STZ_MG_ERR_NONFINITE, "residual is not finite");
+    return v;
+}
+
+double rhs_norm(stz_mg_handle h) {
+    if (h->bnorm < 0) {
+        // |b| via the residual kernel with x = 0 is wasteful; use a dedicated pass
+        const Geom &g = h->geo[0];
+        double *zero = h->L64[0].res;
+        CK(cudaMemsetAsync(zero, 0, 3 * (size_t)g.npad * sizeof(double), h->st));
+        launch_residual<double, double>(h->op64[0], g, h->L64[0].r, zero, (double *)nullptr, h->partial, h->dscal,
+                                        h->st);
+        check_launch();
+        CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        h->bnorm = std::sqrt(h->hscal[0]);
+        if (!std::isfinite(h->bnorm)) fail(STZ_MG_ERR_NONFINITE, "right-hand side is not finite");
+    }
+    return h->bnorm;
+}
+
+// One mixed-precision defect-correction step with k FP32 V-cycles:
+// r32 = b - A x (FP64 residual rounded to FP32), e = 0, k cycles on A e = r32,
+// x += e in FP64.
+void mixed_step(stz_mg_handle h, int k) {
+    const Geom &g = h->geo[0];
+    const size_t n3 = 3 * (size_t)g.npad;
+    CK(cudaMemsetAsync(h->L32[0].x, 0, n3 * sizeof(float), h->st));
+    run_vcycle32(h, k);
+    launch_add_correction(h->L64[0].x, h->L32[0].x, n3, h->st);
+    check_launch();
+}
+
+void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double *relres_out) {
+    need_setup(h);
+    const double bn = rhs_norm(h);
+    const double target = tol * (bn > 0 ? bn : 1.0);
+    int cycles = 0;
+    double rsq;
+    if (h->d.precision == STZ_MG_FP64) {
+        rsq = top_residual_sq(h, nullptr);
+        while (std::sqrt(rsq) > target && cycles < max_cycles) {
+            run_vcycle64(h, 1);
+            cycles++;
+            rsq = top_residual_sq(h, nullptr);
+        }
+    } else {
+        // defect correction: each step solves A e = b - A x with FP32 V-cycles;
+        // the number of cycles per step follows the observed contraction so
+        // that each step gains about five digits (the FP32 floor) or reaches
+        // the tolerance.
+        rsq = top_residual_sq(h, h->L32[0].r);
+        double rn = std::sqrt(rsq), rho = 0.2;
+        int k = 3;
+        while (rn > target && cycles < max_cycles) {
+            k = std::max(1, std::min(k, max_cycles - cycles));
+            mixed_step(h, k);
+            cycles += k;
+            rsq = top_residual_sq(h, h->L32[0].r);
+            double rn_new = std::sqrt(rsq);
+            double gain = rn_new / rn;
+            if (gain > 0 && gain < 1) rho = std::min(0.9, std::max(1e-3, std::pow(gain, 1.0 / k)));
+            else rho = 0.9;
+            rn = rn_new;
+            double want = std::max(target / rn, 2e-6);
+            k = (int)std::ceil(std::log(want) / std::log(rho) - 1e-9);
+            k = std::max(1, std::min(k, 12));
+        }
+    }
+    if (cycles_out) *cycles_out = cycles;
+    double rel = std::sqrt(rsq) / (bn > 0 ? bn : 1.0);
+    if (relres_out) *relres_out = rel;
+    if (std::sqrt(rsq) > target)
+        fail(STZ_MG_ERR_NOCONV, "not converged: relative residual %.3e after %d cycles", rel, cycles);
+}
+
+}  // namespace
+
+// ====================================================================== C-ABI
+extern "C" {
+
+void stz_mg_desc_default(stz_mg_desc *d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof *d);
+    d->precision = STZ_MG_FP64;
+    d->v_down = 2;
+    d->v_up = 2;
+    d->max_coarse = 16;
+    d->bottom = STZ_MG_BOTTOM_DIRECT;
+    d->bottom_sweeps = 24;
+    d->device = 0;
+    d->stream = nullptr;
+}
+
+const char *stz_mg_last_error(void) { return g_last_error.c_str(); }
+
+int stz_mg_create(const stz_mg_desc *desc, stz_mg_handle *out) {
+    if (!desc || !out) return set_error(STZ_MG_ERR_ARG, "null argument");
+    *out = nullptr;
+    const stz_mg_desc &d = *desc;
+    if (d.m < 1 || d.n < 1 || d.o < 1) return set_error(STZ_MG_ERR_ARG, "grid sizes must be positive");
+    if (d.precision != STZ_MG_FP64 && d.precision != STZ_MG_MIXED) return set_error(STZ_MG_ERR_ARG, "bad precision");
+    if (d.bottom != STZ_MG_BOTTOM_DIRECT && d.bottom != STZ_MG_BOTTOM_GS) return set_error(STZ_MG_ERR_ARG, "bad bottom");
+    if (d.v_down < 0 || d.v_up < 0 || d.bottom_sweeps < 0 || d.max_coarse < 1)
+        return set_error(STZ_MG_ERR_ARG, "negative sweep count or max_coarse < 1");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return set_error(STZ_MG_ERR_CUDA, "no CUDA device available");
+    if (d.device < 0 || d.device >= ndev) return set_error(STZ_MG_ERR_ARG, "bad device ordinal %d", d.device);
+    stz_mg_handle h = new (std::nothrow) stz_mg_handle_s();
+    if (!h) return set_error(STZ_MG_ERR_OOM, "host allocation failed");
+    h->d = d;
+    int rc = guarded(h, [&] {
+        if (d.stream) {
+            h->st = (cudaStream_t)d.stream;
+        } else {
+            CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+            h->own_stream = true;
+        }
+        build_geometry(h);
+        alloc_fields(h);
+        sync(h);
+    });
+    if (rc != STZ_MG_OK) {
+        stz_mg_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return STZ_MG_OK;
+}
+
+int stz_mg_destroy(stz_mg_handle h) {
+    if (!h) return STZ_MG_OK;
+    cudaSetDevice(h->d.device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    release_graphs(h);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->hscal) cudaFreeHost(h->hscal);
+    if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return STZ_MG_OK;
+}
+
+int stz_mg_set_stencil_const(stz_mg_handle h, const double *stencil, const double *fix) {
+    if (!h || !stencil || !fix) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        invalidate(h);
+        set_const_op(h, stencil, fix);
+    });
+}
+
+int stz_mg_set_stencil_points(stz_mg_handle h, const double *A, int where) {
+    if (!h || !A) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        invalidate(h);
+        const Geom &g = h->geo[0];
+        const size_t n = 243 * npts(g);
+        const double *src = to_device(h, A, n, where);
+        require_finite(h, src, n, "stencil");
+        if (!h->top_coef64) {
+            h->top_coef64 = h->alloc<double>(243 * (size_t)g.npad);
+            h->top_dinv64 = h->alloc<double>(9 * (size_t)g.npad);
+            if (h->d.precision == STZ_MG_MIXED) {
+                h->top_coef32 = h->alloc<float>(243 * (size_t)g.npad);
+                h->top_dinv32 = h->alloc<float>(9 * (size_t)g.npad);
+            }
+        }
+        CK(cudaMemsetAsync(h->top_coef64, 0, 243 * (size_t)g.npad * sizeof(double), h->st));
+        launch_coef_nat_to_cb(g, src, h->top_coef64, h->st);
+        check_launch();
+        // Dirichlet nodes keep only their centre block (fill_entries stores one entry)
+        h->op64[0] = LevelOp<double>{};
+        h->op64[0].kind = OP_DENSE;
+        h->op64[0].dop.coef = h->top_coef64;
+        h->op64[0].dop.dinv = h->top_dinv64;
+        h->op32[0] = LevelOp<float>{};
+        h->op32[0].kind = OP_DENSE;
+        h->top_kind = OP_DENSE;
+        sync(h);
+    });
+}
+
+int stz_mg_set_coeffs_lame(stz_mg_handle h, const double *mu, const double *lam, double dx, double dy, double dz,
+                           double dt, int where) {
+    if (!h || !mu || !lam) return set_error(STZ_MG_ERR_ARG, "null argument");
+    if (!(dx > 0 && dy > 0 && dz > 0 && std::isfinite(dt))) return set_error(STZ_MG_ERR_ARG, "bad spacing or dt");
+    return guarded(h, [&] {
+        invalidate(h);
+        const Geom &g = h->geo[0];
+        const size_t n = npts(g);
+        if (!h->mu64) {
+            h->mu64 = h->alloc<double>(g.npad);
+            h->lam64 = h->alloc<double>(g.npad);
+            CK(cudaMemsetAsync(h->mu64, 0, g.npad * sizeof(double), h->st));
+            CK(cudaMemsetAsync(h->lam64, 0, g.npad * sizeof(double), h->st));
+            if (h->d.precision == STZ_MG_MIXED) {
+                h->mu32 = h->alloc<float>(g.npad);
+                h->lam32 = h->alloc<float>(g.npad);
+            }
+        }
+        const double *s1 = to_device(h, mu, n, where);
+        require_finite(h, s1, n, "mu");
+        launch_scalar_nat_to_cb<double>(g, s1, h->mu64, h->st);
+        sync(h);
+        const double *s2 = to_device(h, lam, n, where);
+        require_finite(h, s2, n, "lambda");
+        launch_scalar_nat_to_cb<double>(g, s2, h->lam64, h->st);
+        check_launch();
+        h->op64[0] = LevelOp<double>{};
+        h->op64[0].kind = OP_LAME;
+        h->op64[0].lop = LameOp<double>{h->mu64, h->lam64, dx, dy, dz, dt};
+        if (h->d.precision == STZ_MG_MIXED) {
+            launch_convert(h->mu64, h->mu32, g.npad, h->st);
+            launch_convert(h->lam64, h->lam32, g.npad, h->st);
+            check_launch();
+            h->op32[0] = LevelOp<float>{};
+            h->op32[0].kind = OP_LAME;
+            h->op32[0].lop = LameOp<float>{h->mu32, h->lam32, (float)dx, (float)dy, (float)dz, (float)dt};
+        }
+        h->top_kind = OP_LAME;
+        sync(h);
+    });
+}
+
+int stz_mg_setup(stz_mg_handle h) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] { setup(h); });
+}
+
+int stz_mg_set_rhs(stz_mg_handle h, const double *r, int where) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const double *src = to_device(h, r, 3 * npts(g), where);
+        launch_nat_to_cb<double>(g, src, h->L64[0].r, h->st);
+        check_launch();
+        h->bnorm = -1.0;
+        if (where == STZ_MG_HOST) sync(h);
+    });
+}
+
+int stz_mg_set_x(stz_mg_handle h, const double *x, int where) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const double *src = to_device(h, x, 3 * npts(g), where);
+        launch_nat_to_cb<double>(g, src, h->L64[0].x, h->st);
+        check_launch();
+        if (where == STZ_MG_HOST) sync(h);
+    });
+}
+
+int stz_mg_get_x(stz_mg_handle h, double *x, int where) {
+    if (!h || !x) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const size_t n = 3 * npts(g);
+        if (where == STZ_MG_DEVICE) {
+            launch_cb_to_nat<double>(g, h->L64[0].x, x, h->st);
+            check_launch();
+        } else {
+            double *d = staging(h, n);
+            launch_cb_to_nat<double>(g, h->L64[0].x, d, h->st);
+            check_launch();
+            CK(cudaMemcpyAsync(x, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            sync(h);
+        }
+    });
+}
+
+int stz_mg_vcycle(stz_mg_handle h) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        if (h->d.precision == STZ_MG_FP64) {
+            run_vcycle64(h, 1);
+        } else {
+            top_residual_sq(h, h->L32[0].r);
+            mixed_step(h, 1);
+        }
+        sync(h);
+    });
+}
+
+int stz_mg_solve(stz_mg_handle h, double rel_tol, int max_cycles, int *cycles, double *relres) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    if (!(rel_tol > 0) || max_cycles < 0) return set_error(STZ_MG_ERR_ARG, "bad tolerance or cycle cap");
+    return guarded(h, [&] { solve(h, rel_tol, max_cycles, cycles, relres); });
+}
+
+int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        double rs = top_residual_sq(h, nullptr);
+        if (rnorm) *rnorm = std::sqrt(rs);
+        if (bnorm) *bnorm = rhs_norm(h);
+    });
+}
+
+int stz_mg_l2_error_all(stz_mg_handle h, double *out) {
+    if (!h || !out) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        need_setup(h);
+        const Geom &g = h->geo[0];
+        const size_t n = 3 * npts(g);
+        launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L64[0].res, nullptr, nullptr,
+                                        h->st);
+        check_launch();
+        double *nat = staging(h, n);
+        launch_cb_to_nat<double>(g, h->L64[0].res, nat, h->st);
+        std::vector<double> v(n);
+        CK(cudaMemcpyAsync(v.data(), nat, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        double s = 0;
+        for (size_t p = 0; p < n; p += 3) {
+            double q = v[p] * v[p] + v[p + 1] * v[p + 1] + v[p + 2] * v[p + 2];
+            s += q * q;
+        }
+        *out = s;
+    });
+}
+
+int stz_mg_num_levels(stz_mg_handle h, int *nlevels) {
+    if (!h || !nlevels) return set_error(STZ_MG_ERR_ARG, "null argument");
+    *nlevels = h->nlev;
+    return STZ_MG_OK;
+}
+
+int stz_mg_level_dims(stz_mg_handle h, int level, int *dims3) {
+    if (!h || !dims3) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        check_level(h, level);
+        dims3[0] = h->geo[level].m; dims3[1] = h->geo[level].n; dims3[2] = h->geo[level].o;
+    });
+}
+
+int stz_mg_level_operator(stz_mg_handle h, int level, double *A, int *S) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        const size_t N = npts(g);
+        if (A) {
+            double *dcoef = nullptr;
+            const double *src;
+            if (level == 0 && h->top_kind != OP_DENSE) {
+                dcoef = h->alloc<double>(243 * (size_t)g.npad);
+                launch_expand_dense(h->op64[0], g, dcoef, h->st);
+                src = dcoef;
+            } else {
+                src = level == 0 ? h->top_coef64 : h->L64[level].coef;
+            }
+            double *nat = staging(h, 243 * N);
+            launch_coef_cb_to_nat(g, src, nat, h->st);
+            check_launch();
+            CK(cudaMemcpyAsync(A, nat, 243 * N * sizeof(double), cudaMemcpyDefault, h->st));
+            sync(h);
+            h->release(dcoef);
+        }
+        if (S) {
+            int *tmp = h->alloc<int>(6 * N);
+            launch_bounds_cb_to_nat(g, h->S[level], tmp, h->st);
+            check_launch();
+            CK(cudaMemcpyAsync(S, tmp, 6 * N * sizeof(int), cudaMemcpyDefault, h->st));
+            sync(h);
+            h->release(tmp);
+        }
+    });
+}
+
+int stz_mg_level_set_field(stz_mg_handle h, int level, int which, const double *v, int where) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        const double *src = to_device(h, v, 3 * npts(g), where);
+        double *dst = which == STZ_MG_FIELD_X ? h->L64[level].x : h->L64[level].r;
+        launch_nat_to_cb<double>(g, src, dst, h->st);
+        check_launch();
+        if (level == 0 && which == STZ_MG_FIELD_R) h->bnorm = -1.0;
+        sync(h);
+    });
+}
+
+int stz_mg_level_get_field(stz_mg_handle h, int level, int which, double *v, int where) {
+    if (!h || !v) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        const size_t n = 3 * npts(g);
+        const double *src = which == STZ_MG_FIELD_X ? h->L64[level].x : h->L64[level].r;
+        double *d = where == STZ_MG_DEVICE ? v : staging(h, n);
+        launch_cb_to_nat<double>(g, src, d, h->st);
+        check_launch();
+        if (where != STZ_MG_DEVICE) CK(cudaMemcpyAsync(v, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_level_gauss_seidel(stz_mg_handle h, int level, int sweeps) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        for (int s = 0; s < sweeps; s++)
+            launch_gs_sweep<double>(h->op64[level], h->geo[level], h->L64[level].r, h->L64[level].x, h->st);
+        sync(h);
+    });
+}
+
+int stz_mg_level_restriction(stz_mg_handle h, int level) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        if (level < 1) fail(STZ_MG_ERR_ARG, "restriction target must be a coarse level");
+        const int f = level - 1;
+        launch_residual<double, double>(h->op64[f], h->geo[f], h->L64[f].r, h->L64[f].x, h->L64[f].res, nullptr,
+                                        nullptr, h->st);
+        launch_restriction<double>(h->geo[f], h->geo[level], h->L64[f].res, h->L64[level].r, h->st);
+        CK(cudaMemsetAsync(h->L64[level].x, 0, 3 * (size_t)h->geo[level].npad * sizeof(double), h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_level_interpolation(stz_mg_handle h, int level) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        if (level < 1) fail(STZ_MG_ERR_ARG, "interpolation source must be a coarse level");
+        launch_interpolation<double>(h->geo[level - 1], h->geo[level], h->L64[level].x, h->L64[level - 1].x, h->st);
+        sync(h);
+    });
+}
+
+int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq, int where) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        launch_residual<double, double>(h->op64[level], g, h->L64[level].r, h->L64[level].x, h->L64[level].res,
+                                        h->partial, h->dscal, h->st);
+        check_launch();
+        CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        if (out) {
+            const size_t n = 3 * npts(g);
+            double *d = where == STZ_MG_DEVICE ? out : staging(h, n);
+            launch_cb_to_nat<double>(g, h->L64[level].res, d, h->st);
+            check_launch();
+            if (where != STZ_MG_DEVICE) CK(cudaMemcpyAsync(out, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        }
+        sync(h);
+        if (sumsq) *sumsq = h->hscal[0];
+    });
+}
+
+}  // extern "C"

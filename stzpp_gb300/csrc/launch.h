@@ -1,0 +1,72 @@
+// Host-side declarations of the kernel launchers of the GB300 multigrid.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace stzmg {
+
+// One level's operator as the kernels see it.
+template <typename T>
+struct LevelOp {
+    OpKind kind;
+    ConstOp<T> cop;
+    LameOp<T> lop;
+    DenseOp<T> dop;
+};
+
+// smooth.cu
+template <typename T>
+void launch_gs_colour(const LevelOp<T> &op, const Geom &g, int q, const T *r, T *x, cudaStream_t st);
+template <typename T>
+void launch_gs_sweep(const LevelOp<T> &op, const Geom &g, const T *r, T *x, cudaStream_t st);
+int residual_blocks(const Geom &g);
+// res = r - A x (res may be null); when partial is non-null, per-block sums of
+// |res|^2 go to partial[residual_blocks(g)] and, when out is non-null, their
+// total to out[0].
+template <typename T, typename R>
+void launch_residual(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, R *res, double *partial,
+                     double *out, cudaStream_t st);
+
+// transfer.cu
+template <typename T>
+void launch_restriction(const Geom &gf, const Geom &gc, const T *res_f, T *r_c, cudaStream_t st);
+template <typename T>
+void launch_interpolation(const Geom &gf, const Geom &gc, const T *x_c, T *x_f, cudaStream_t st);
+// natural-order AoS vec3 (double) <-> colour-blocked SoA
+template <typename T>
+void launch_nat_to_cb(const Geom &g, const double *nat, T *cb, cudaStream_t st);
+template <typename T>
+void launch_cb_to_nat(const Geom &g, const T *cb, double *nat, cudaStream_t st);
+// natural-order scalar (double) -> colour-blocked scalar
+template <typename T>
+void launch_scalar_nat_to_cb(const Geom &g, const double *nat, T *cb, cudaStream_t st);
+// natural-order dense coefficients (npts x 243 doubles) -> colour-blocked SoA (243 x npad)
+void launch_coef_nat_to_cb(const Geom &g, const double *nat, double *cb, cudaStream_t st);
+void launch_coef_cb_to_nat(const Geom &g, const double *cb, double *nat, cudaStream_t st);
+void launch_convert(const double *src, float *dst, size_t n, cudaStream_t st);
+// x64 += e32 over n elements
+void launch_add_correction(double *x, const float *e, size_t n, cudaStream_t st);
+// x = Ainv r on the bottom level: Ainv is (3N)^2 column-major (Ainv_T[col*3N+row]),
+// nat_slot maps natural node index -> slot.
+template <typename T>
+void launch_bottom_direct(int nrow, const double *ainv_t, const int *nat_slot, int npad, const T *r, T *x,
+                          cudaStream_t st);
+void launch_scale(double *v, double s, size_t n, cudaStream_t st);
+
+// rat.cu
+// Galerkin coarse operator A_c = (1/8) P^T A P into a dense SoA field (243 x npad_c).
+void launch_rat(const LevelOp<double> &fine, const Geom &gf, const Geom &gc, double *coef_c, cudaStream_t st);
+// dense 27-block SoA copy of any operator (top level export)
+void launch_expand_dense(const LevelOp<double> &op, const Geom &g, double *coef, cudaStream_t st);
+// inverse of every centre block; bad[0] set to 1 on a singular/non-finite block
+template <typename T>
+void launch_dense_dinv(const Geom &g, const T *coef, T *dinv, int *bad, cudaStream_t st);
+// RAT box bounds (6 ints per slot) of the coarse level from the fine bounds
+// (fill_rat_bounds); fine_S null means the top level's interior/boundary boxes.
+void launch_rat_bounds(const Geom &gf, const int *fine_S, const Geom &gc, int *S_c, int *bad, cudaStream_t st);
+void launch_top_bounds(const Geom &g, int *S, cudaStream_t st);
+void launch_bounds_cb_to_nat(const Geom &g, const int *S, int *nat, cudaStream_t st);
+
+}  // namespace stzmg

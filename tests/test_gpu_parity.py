@@ -1,0 +1,174 @@
+"""GPU parity: the CUDA path through the C-ABI against the oracle.
+
+The oracle is the C restatement of the reference multigrid (oracle/), itself
+pinned to the compiled reference by tests/test_oracle.py and the golden
+fixtures.  Kernels are compared one by one on the same seeded inputs (box
+bounds exactly; coefficients, sweeps and transfers to FP64 round-off), then
+whole V-cycles with the same smoother order, then converged solutions against
+the reference's own lexicographic solver (relative L2 error <= 1e-9).
+"""
+import numpy as np
+import pytest
+
+from oracle import problem as P
+
+pytestmark = pytest.mark.gpu
+
+# round-off tolerance for one kernel in FP64: max-norm error relative to the
+# max-norm of the oracle's output
+KERNEL_RTOL = 1e-13
+# converged-solution tolerance of the projection solve (relative L2)
+SOLUTION_RTOL = 1e-9
+
+GRIDS = [
+    ((16, 16, 17), (True, True, False), "const"),
+    ((16, 16, 17), (True, True, False), "points"),
+    ((16, 16, 17), (True, True, False), "lame"),
+    ((12, 10, 9), (False, False, False), "const"),
+    ((16, 12, 10), (True, False, False), "const"),
+]
+
+
+def rel_max(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def build_pair(dims, per, kind, oracle_port, max_coarse=16, precision="fp64", bottom="direct"):
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    mg = sg.Multigrid(dims, per, precision=precision, max_coarse=max_coarse, bottom=bottom)
+    if kind == "const":
+        st, fix = P.elastic_stencil_const(1.0, 2.0, dx, dy, dz)
+        ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=max_coarse)
+        st_gpu, fix_gpu = sg.elastic_stencil(1.0, 2.0, dx, dy, dz)
+        mg.setup_matrices(stencil=st_gpu, fix=fix_gpu)
+    else:
+        mu = P.lognormal_mu(1, m, n, o)
+        pts = P.elastic_stencil_points(mu, 2 * mu, dx, dy, dz, per)
+        ref = oracle_port.PortMultigrid(dims, per, points=pts, max_coarse=max_coarse)
+        if kind == "points":
+            mg.setup_matrices(points=pts)
+        else:
+            mg.setup_matrices(mu=mu.reshape(-1), lam=(2 * mu).reshape(-1), spacing=(dx, dy, dz))
+    return mg, ref
+
+
+@pytest.mark.parametrize("dims,per,kind", GRIDS)
+def test_hierarchy_and_operators(dims, per, kind, oracle_port):
+    mg, ref = build_pair(dims, per, kind, oracle_port)
+    assert mg.nlevels == ref.nlevels
+    for l in range(mg.nlevels):
+        assert mg.level_dims(l) == ref.level_dims(l)
+        A, S = mg.level_operator(l)
+        assert np.array_equal(S, ref.level_S(l)), f"box bounds differ on level {l}"
+        Ar = ref.level_A(l)
+        assert rel_max(A, Ar) < KERNEL_RTOL, f"level {l} coefficients: {rel_max(A, Ar):.3e}"
+    mg.close()
+
+
+@pytest.mark.parametrize("dims,per,kind", GRIDS)
+def test_level_kernels(dims, per, kind, oracle_port):
+    mg, ref = build_pair(dims, per, kind, oracle_port)
+    rng = np.random.default_rng(7)
+    for l in range(mg.nlevels):
+        N = mg.level_npts(l)
+        x = rng.standard_normal((N, 3))
+        r = rng.standard_normal((N, 3))
+        for M in (mg,):
+            M.level_set_field(l, "x", x)
+            M.level_set_field(l, "r", r)
+        ref.set_field(l, "x", x)
+        ref.set_field(l, "r", r)
+        # residual
+        res_g, sq_g = mg.residual(l)
+        res_o, sq_o = ref.residual(l)
+        assert rel_max(res_g, res_o) < KERNEL_RTOL
+        assert abs(sq_g - sq_o) <= 1e-12 * sq_o
+        # one 8-colour sweep
+        mg.gauss_seidel(l, 1)
+        ref.gauss_seidel(l, 1, smoother="mc8")
+        assert rel_max(mg.level_get_field(l, "x"), ref.get_field(l, "x")) < KERNEL_RTOL
+        if l + 1 < mg.nlevels:
+            mg.restriction(l + 1)
+            ref.restriction(l + 1)
+            assert rel_max(mg.level_get_field(l + 1, "r"), ref.get_field(l + 1, "r")) < KERNEL_RTOL
+            assert not mg.level_get_field(l + 1, "x").any()
+            xc = rng.standard_normal((mg.level_npts(l + 1), 3))
+            mg.level_set_field(l + 1, "x", xc)
+            ref.set_field(l + 1, "x", xc)
+            mg.interpolation(l + 1)
+            ref.interpolation(l + 1)
+            assert rel_max(mg.level_get_field(l, "x"), ref.get_field(l, "x")) < KERNEL_RTOL
+    mg.close()
+
+
+@pytest.mark.parametrize("dims,per,kind", GRIDS[:4])
+def test_vcycle_iterates(dims, per, kind, oracle_port):
+    """Whole V-cycles: same smoother order (8 colours), same direct bottom."""
+    mg, ref = build_pair(dims, per, kind, oracle_port)
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, dx, dy, dz)
+    mg.setup_fields(r=b)
+    ref.set_field(0, "r", b)
+    ref.set_field(0, "x", np.zeros_like(b))
+    for c in range(3):
+        mg.v_cycle()
+        ref.v_cycle(bottom="direct", smoother="mc8")
+        xg, xo = mg.get_x(), ref.get_field(0, "x")
+        assert rel_max(xg, xo) < 1e-11, f"cycle {c}: {rel_max(xg, xo):.3e}"
+    mg.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["const", "lame"])
+def test_solution_matches_reference_solver(precision, kind, oracle_port):
+    """32x32x33 (dx = 1/32), periodic x,y, Dirichlet z: converged solution of the
+    GPU solve against the reference's lexicographic solver with its own
+    hierarchy (coarsest level <= 1024 nodes, 24 GS sweeps at the bottom)."""
+    import stzpp_gb300 as sg
+    dims, per = (32, 32, 33), (True, True, False)
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, dx, dy, dz)
+    if kind == "const":
+        st, fix = P.elastic_stencil_const(1.0, 2.0, dx, dy, dz)
+        ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=1024)
+    else:
+        mu = P.lognormal_mu(1, m, n, o)
+        ref = oracle_port.PortMultigrid(dims, per, points=P.elastic_stencil_points(mu, 2 * mu, dx, dy, dz, per),
+                                        max_coarse=1024)
+    ref.set_field(0, "r", b)
+    ref.set_field(0, "x", np.zeros_like(b))
+    cyc_ref, hist = ref.solve(1e-13, 200, bottom="gs", smoother="lex")
+    x_ref = ref.get_field(0, "x")
+    with sg.Multigrid(dims, per, precision=precision) as mg:
+        if kind == "const":
+            mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, dx, dy, dz))
+        else:
+            mg.setup_matrices(mu=mu.reshape(-1), lam=(2 * mu).reshape(-1), spacing=(dx, dy, dz))
+        mg.setup_fields(r=b)
+        cycles, rel = mg.solve(1e-10, 100)
+        x = mg.get_x()
+        rn, bn = mg.residual_norm()
+    assert rel <= 1e-10 and rn / bn <= 1e-10
+    err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+    assert err <= SOLUTION_RTOL, f"{precision}/{kind}: {cycles} cycles, error {err:.3e}"
+
+
+def test_reference_hierarchy_gs_bottom(oracle_port):
+    """The reference's own cycle shape (coarsest <= 1024 nodes, 24 GS sweeps)."""
+    mg, ref = build_pair((32, 32, 33), (True, True, False), "const", oracle_port, max_coarse=1024, bottom="gs")
+    assert mg.nlevels == ref.nlevels == 3
+    m, n, o = 32, 32, 33
+    dx, dy, dz = P.grid_spacing(m, n, o, (True, True, False))
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, (True, True, False)), m, n, o, (True, True, False), dx, dy, dz)
+    mg.setup_fields(r=b)
+    ref.set_field(0, "r", b)
+    ref.set_field(0, "x", np.zeros_like(b))
+    for c in range(2):
+        mg.v_cycle()
+        ref.v_cycle(bottom="gs", smoother="mc8")
+    assert rel_max(mg.get_x(), ref.get_field(0, "x")) < 1e-11
+    mg.close()
