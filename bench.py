@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Benchmark: stzpp's quasi-static projection solve on one GB300.
+
+Workload (the 257^3 problem): 256 x 256 x 257 nodes -- periodic x and y with
+256 cells, Dirichlet plates in z with 256 cells -- dx = 1/256, the elasticity
+operator with mu = 1, lambda = 2 (the shared 27-block stencil of
+shear_sim_3d::set_up_stencil_base), right-hand side = node divergence of a
+random symmetric cell tensor field with i.i.d. N(0, 1e-3) entries (seed 0),
+zero initial guess, V-cycles until |b - Ax| / |b| <= 1e-10.
+
+One step = one solve.  `value` is ms per solve in mixed precision (FP32
+V-cycles inside FP64 defect correction) with every input resident in HBM;
+`e2e` is the same solve through the C-ABI from pinned host buffers (RHS
+host->device, solution device->host inside the timed region).  The plain FP64
+GPU solve is timed beside it.  Fine-level vectors are 404 MB each (larger
+than the 129 MB L2), so no L2 flush is needed between steps.
+
+--impl reference times the reference algorithm on the host cores (the
+compiled reference when present, else the C restatement in oracle/) on a
+bounded sample and prints the same metric.
+
+Runs as N independent replicas under torchrun (--gpus N): the solve is not
+sharded in this build.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/solve to rel. residual 1e-10 at 257³, mixed vs FP64 on GPU; smoother % HBM"
+DIMS = (256, 256, 257)
+PERIODIC = (True, True, False)
+TOL = 1e-10
+WORKLOAD = ("quasi-static projection solve, 256x256x257 nodes (257^3 problem: periodic x,y, Dirichlet z), "
+            "mu=1, lambda=2, dx=1/256, RHS = divergence of N(0,1e-3) cell strain (seed 0), x0 = 0, "
+            "to relative residual 1e-10")
+CPU_SAMPLE_DIMS = (64, 64, 65)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(name):
+    """DRAM bytes per launch of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(name)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.flush()
+        rows = [l.strip().split(",") for l in open(self.out.name) if l.strip()]
+        os.unlink(self.out.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            r = [v.strip() for v in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(steps=1):
+    """The reference algorithm (lexicographic GS, coarsest level <= 1024 nodes,
+    24 bottom sweeps) on one host core, at 64x64x65 with the same operator and
+    right-hand side distribution, scaled to 256x256x257 by the node count
+    (multigrid work is linear in the nodes; cycle counts are grid-independent)."""
+    from oracle import problem as P
+    try:
+        from oracle import refpy
+        use_ref = refpy.available()
+    except Exception:
+        use_ref = False
+    m, n, o = CPU_SAMPLE_DIMS
+    dx, dy, dz = P.grid_spacing(m, n, o, PERIODIC)
+    st, fix = P.elastic_stencil_const(1.0, 2.0, dx, dy, dz)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, PERIODIC), m, n, o, PERIODIC, dx, dy, dz)
+    if use_ref:
+        try:
+            M = refpy.RefMultigrid((m, n, o), PERIODIC, stencil=st, fix=fix, max_coarse=1024)
+            kind = "reference"
+        except Exception:
+            use_ref = False
+    if not use_ref:
+        from oracle import port
+        if not port.available():
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+        M = port.PortMultigrid((m, n, o), PERIODIC, stencil=st, fix=fix, max_coarse=1024)
+        kind = "port"
+    times, cycles = [], 0
+    for _ in range(steps):
+        M.set_field(0, "r", b)
+        M.set_field(0, "x", np.zeros_like(b))
+        t = time.perf_counter()
+        cycles, hist = (M.solve(TOL, 200) if kind == "reference" else M.solve(TOL, 200, bottom="gs", smoother="lex"))
+        times.append(time.perf_counter() - t)
+    scale = (DIMS[0] * DIMS[1] * DIMS[2]) / float(m * n * o)
+    ms = statistics.median(times) * 1e3 * scale
+    return {"value": ms, "unit": "ms", "cores": 1, "kind": kind,
+            "sample": (f"full solve to 1e-10 at {m}x{n}x{o} ({cycles} V-cycles, "
+                       f"{statistics.median(times):.2f} s on 1 core), scaled by the node ratio {scale:.1f}"),
+            "host_cores_available": os.cpu_count()}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cb = cpu_baseline(steps=max(1, min(args.steps, 3)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["value"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "solver": "reference multigrid<vec3,mat3>, lexicographic GS, "
+                                                      "V(2+i,2+i), 24 GS sweeps at the <=1024-node bottom"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import stzpp_gb300 as sg
+    from stzpp_gb300 import problems
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if dist.is_nccl_available() else "gloo")
+    dims, per = DIMS, PERIODIC
+    npts = dims[0] * dims[1] * dims[2]
+    spacing = problems.grid_spacing(dims, per)
+    stencil, fix = sg.elastic_stencil(1.0, 2.0, *spacing)
+    eps = problems.random_strain(0, dims, per)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if dist is None:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------------------------------------------------- mixed solve
+    mg = sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, device=local, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    mg.setup_matrices(stencil=stencil, fix=fix)
+    torch.cuda.synchronize()
+    setup_ms = (time.perf_counter() - t0) * 1e3
+    mg.set_rhs_divergence(eps, spacing)
+    b_dev = torch.empty(3 * npts, dtype=torch.float64, device="cuda")
+    mg.get_rhs(b_dev)
+    zero = torch.zeros_like(b_dev)
+
+    def step(M):
+        M.set_x(zero)
+        return M.solve(TOL, 200)
+
+    for _ in range(args.warmup):
+        step(mg)
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    cycles = 0
+    for _ in range(args.steps):
+        cycles, rel = step(mg)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms_mixed = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    vcyc, nres, launches = mg.solve_stats()
+    x_mixed = torch.empty_like(b_dev)
+    mg.get_x(x_mixed)
+
+    # ------------------------------------------------- end to end (C-ABI)
+    b_host = torch.empty(3 * npts, dtype=torch.float64, pin_memory=True)
+    b_host.copy_(b_dev)
+    x_host = torch.empty(3 * npts, dtype=torch.float64, pin_memory=True)
+    e2e_steps = max(2, args.steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        mg.set_rhs(b_host)          # host -> device
+        mg.set_x(zero)
+        mg.solve(TOL, 200)
+        mg.get_x(x_host)            # device -> host
+    barrier()
+    ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps)
+
+    # -------------------------------------------------- kernel roofline
+    hbm, hbm_kind = peaks()
+    kern = {}
+    for name, kid, lvl in (("gs_colour_l0", sg.mg.K_GS_COLOUR, 0), ("gs_colour_l1", sg.mg.K_GS_COLOUR, 1),
+                           ("residual_l0_fp32", sg.mg.K_RESIDUAL, 0), ("restrict_l1", sg.mg.K_RESTRICT, 1),
+                           ("interp_l1", sg.mg.K_INTERP, 1), ("residual_fp64", sg.mg.K_RESIDUAL64, 0)):
+        ms, work = mg.time_kernel(kid, lvl, reps=20)
+        kern[name] = (ms, work)
+    # share of a solve: the fine smoother runs (v_down + v_up) sweeps x 8 colours per V-cycle
+    gs_launches = 4 * 8 * vcyc
+    gs_ms, gs_bytes = kern["gs_colour_l0"]
+    achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
+    r64_ms, r64_flops = kern["residual_fp64"]
+    roofline = {"kernel": "gs_const_kernel<float> (fine-level 8-colour GS, one colour pass)",
+                "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "peak_kind": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if hbm_kind == "measured" else hbm_kind,
+                "traffic": traffic_from_profile("gs_const_kernel<float>"),
+                "algorithmic_bytes_per_launch": gs_bytes, "ms_per_launch": gs_ms,
+                "launches_per_solve": gs_launches,
+                "share_of_solve_est": gs_launches * gs_ms / ms_mixed}
+    smoother = {name: {"ms_per_launch": v[0], "GB/s": v[1] / (v[0] * 1e-3) / 1e9,
+                       "frac_hbm": v[1] / (v[0] * 1e-3) / 1e9 / hbm}
+                for name, v in kern.items() if name != "residual_fp64"}
+    smoother["residual_fp64"] = {"ms_per_launch": r64_ms, "FP64 TFLOP/s": r64_flops / (r64_ms * 1e-3) / 1e12,
+                                 "launches_per_solve": nres}
+    mg.close()
+
+    # ------------------------------------------------------ FP64 solve
+    mg64 = sg.Multigrid(dims, per, precision="fp64", sweep_growth=False, device=local, stream=stream.cuda_stream)
+    mg64.setup_matrices(stencil=stencil, fix=fix)
+    mg64.set_rhs(b_dev)
+    steps64 = max(2, args.steps // 2)
+    for _ in range(min(args.warmup, 2)):
+        step(mg64)
+    barrier()
+    e0.record(stream)
+    for _ in range(steps64):
+        cyc64, rel64 = step(mg64)
+    e1.record(stream)
+    barrier()
+    ms_fp64 = max_over_ranks(e0.elapsed_time(e1) / steps64)
+    x64 = torch.empty_like(b_dev)
+    mg64.get_x(x64)
+    mg64.close()
+    err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
+
+    cpu = cpu_baseline(1) if (rank == 0 and world == 1) else None
+    if rank == 0:
+        value = ms_mixed / world
+        line = {
+            "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "dims": list(dims), "precision": "mixed: FP32 V-cycles, FP64 residual/update/bottom",
+                       "cycle": "V(2,2) on every level, 8-colour block GS, RAT coarse operators (plane-invariant storage), FP64 direct solve at 8x8x9",
+                       "replicas": world, "l2": "inputs larger than L2 (fine vectors 404 MB each); no flush needed"},
+            "cycles": cycles, "relres": rel, "setup_ms": setup_ms,
+            "fp64": {"ms_per_solve": ms_fp64, "cycles": cyc64, "relres": rel64},
+            "speedup_vs_fp64": ms_fp64 / ms_mixed, "solution_rel_err_vs_fp64": err,
+            "roofline": roofline, "kernels": smoother,
+            "e2e": {"value": ms_e2e / world, "unit": "ms", "h2d_bytes_per_step": 3 * npts * 8,
+                    "d2h_bytes_per_step": 3 * npts * 8},
+            "gpu_launches": int(launches * args.steps),
+            "clocks": clk,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

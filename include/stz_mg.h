@@ -53,12 +53,14 @@ typedef struct {
     int max_coarse;     /* coarsen while the coarsest level has more nodes (reference: 1024, multigrid.cc:40) */
     int bottom;         /* STZ_MG_BOTTOM_DIRECT (FP64 dense solve) or STZ_MG_BOTTOM_GS */
     int bottom_sweeps;  /* sweeps of the GS bottom solve (reference: 24, common.hh:57) */
+    int sweep_growth;   /* 1: v_down+i / v_up+i-1 sweeps on level i as the reference; 0: v_down / v_up on every level */
     int device;         /* CUDA device ordinal */
     void *stream;       /* cudaStream_t to run on, or NULL for a handle-owned stream */
 } stz_mg_desc;
 
-/* Defaults: FP64, v_down = v_up = 2, max_coarse = 16 (coarsest level of a few
- * nodes, e.g. 2x2x3), direct bottom, 24 bottom sweeps, device 0, own stream. */
+/* Defaults: FP64, v_down = v_up = 2 with the reference's growth, max_coarse =
+ * 1024 (the reference's hierarchy), direct bottom, 24 bottom sweeps, device 0,
+ * own stream. */
 void stz_mg_desc_default(stz_mg_desc *d);
 
 const char *stz_mg_last_error(void);
@@ -95,6 +97,15 @@ int stz_mg_set_rhs(stz_mg_handle h, const double *r, int where);
 int stz_mg_set_x(stz_mg_handle h, const double *x, int where);
 /* The solution, read by the drivers through reg[0]->x0 (shear_sim_3d.cpp:616-674). */
 int stz_mg_get_x(stz_mg_handle h, double *x, int where);
+int stz_mg_get_rhs(stz_mg_handle h, double *r, int where);
+
+/* Right-hand side assembled on the device from a cell-centred symmetric
+ * tensor field: the r_field of shear_sim_3d (shear_sim_3d.hh:283-385, plates
+ * at rest) using calculate_first_order_stresses (shear_sim_3d.cpp:979-998).
+ * eps holds 6 doubles per cell (s11 s12 s13 s22 s23 s33), cells in natural
+ * order; a periodic dimension has as many cells as nodes, a non-periodic one
+ * one fewer.  Dirichlet nodes get 0. */
+int stz_mg_set_rhs_divergence(stz_mg_handle h, const double *eps, double dx, double dy, double dz, int where);
 
 /* multigrid::v_cycle (multigrid.cc:253-297).  In mixed precision one call is
  * one defect-correction step: FP64 residual, one FP32 V-cycle, FP64 update. */
@@ -105,6 +116,11 @@ int stz_mg_vcycle(stz_mg_handle h);
  * residual norm).  cycles = V-cycles run, relres = final relative residual;
  * STZ_MG_ERR_NOCONV when max_cycles is reached first. */
 int stz_mg_solve(stz_mg_handle h, double rel_tol, int max_cycles, int *cycles, double *relres);
+
+/* Counters of the last stz_mg_solve: V-cycles, top-level FP64 residual
+ * evaluations, and kernels this library launched (no counterpart in the
+ * reference; its drivers time v_cycle only, shear_sim_3d.cpp:568-571). */
+int stz_mg_solve_stats(stz_mg_handle h, int *vcycles, int *residuals, long long *kernel_launches);
 
 /* |b - A x|_2 and |b|_2 in FP64 on the top level. */
 int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm);
@@ -130,6 +146,21 @@ int stz_mg_level_restriction(stz_mg_handle h, int level);
 int stz_mg_level_interpolation(stz_mg_handle h, int level);
 /* region::residual (region.cc:1008) of every node, 3*npts doubles (may be NULL), and sum |r|^2 */
 int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq, int where);
+
+/* Measurement hook (no counterpart in the reference): launches one kernel of
+ * the solver `reps` times on the handle's stream between CUDA events and
+ * returns the average time per launch and the algorithmic bytes (or FP64
+ * flops for STZ_MG_K_RESIDUAL64) one launch moves.  Overwrites the level's
+ * work fields.  Kernels run in the handle's solver precision. */
+enum {
+    STZ_MG_K_GS_COLOUR = 0,   /* one colour pass of the smoother (colour 0) */
+    STZ_MG_K_RESIDUAL = 1,    /* residual of a level */
+    STZ_MG_K_RESTRICT = 2,    /* restriction into `level` */
+    STZ_MG_K_INTERP = 3,      /* interpolation from `level` */
+    STZ_MG_K_RESIDUAL64 = 4   /* FP64 top-level residual of the defect correction */
+};
+int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
+                       double *work_per_launch);
 
 #ifdef __cplusplus
 }

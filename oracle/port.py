@@ -41,7 +41,7 @@ def _load():
     lib.so_vcycle.argtypes = [vp, ci, ci]
     lib.so_residual.argtypes = [vp, ci, vp, vp]
     lib.so_solve.argtypes = [vp, ctypes.c_double, ci, ci, ci, vp, vp]
-    lib.so_set_cycle.argtypes = [vp, ci, ci, ci]
+    lib.so_set_cycle.argtypes = [vp, ci, ci, ci, ci]
     _lib = lib
     return lib
 
@@ -118,8 +118,8 @@ class PortMultigrid:
         self._check(_load().so_get_field(self._h, l, {"x": 0, "r": 1}[which], _ptr(v)))
         return v
 
-    def set_cycle(self, v_down=2, v_up=2, bottom_sweeps=24):
-        self._check(_load().so_set_cycle(self._h, v_down, v_up, bottom_sweeps))
+    def set_cycle(self, v_down=2, v_up=2, bottom_sweeps=24, grow=True):
+        self._check(_load().so_set_cycle(self._h, v_down, v_up, bottom_sweeps, int(grow)))
 
     def gauss_seidel(self, l, sweeps=1, smoother="lex"):
         self._check(_load().so_gauss_seidel(self._h, l, sweeps, SMOOTHERS[smoother]))

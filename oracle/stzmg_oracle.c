@@ -46,6 +46,7 @@ typedef struct {
     int nlev;
     lev_t L[MAXLEV];
     int v_down, v_up, bottom_sweeps;
+    int grow;   /* 1: v_down+i / v_up+i-1 sweeps on level i (multigrid.cc:265,288); 0: constant */
     int nbot;
     double *lu;
     int *piv;
@@ -560,7 +561,7 @@ static int direct_bottom(st_t *s) {
 static int vcycle(st_t *s, int smoother, int bottom) {
     int L = s->nlev, i, l;
     for (i = 0; i < L - 1; i++) {
-        for (l = 0; l < s->v_down + i; l++) gs_sweep(&s->L[i], smoother);
+        for (l = 0; l < s->v_down + (s->grow ? i : 0); l++) gs_sweep(&s->L[i], smoother);
         restriction(&s->L[i + 1], &s->L[i]);
     }
     if (bottom == 1) {
@@ -570,7 +571,7 @@ static int vcycle(st_t *s, int smoother, int bottom) {
     }
     for (i = L - 1; i > 0; i--) {
         interpolation(&s->L[i], &s->L[i - 1]);
-        for (l = 0; l < s->v_up + i - 1; l++) gs_sweep(&s->L[i - 1], smoother);
+        for (l = 0; l < s->v_up + (s->grow ? i - 1 : 0); l++) gs_sweep(&s->L[i - 1], smoother);
     }
     return 0;
 }
@@ -604,6 +605,7 @@ int so_create(int m, int n, int o, int xp, int yp, int zp, const double *stencil
     if (!pts && (!stencil || !fix)) return fail("need a stencil and fix block, or per-point stencils");
     st_t *s = xcalloc(1, sizeof(st_t));
     s->v_down = 2; s->v_up = 2; s->bottom_sweeps = 24;   /* multigrid.hh:123, common.hh:57 */
+    s->grow = 1;
     lev_t *F = &s->L[0];
     F->m = m; F->n = n; F->o = o; F->xp = xp != 0; F->yp = yp != 0; F->zp = zp != 0;
     build_fine(F, stencil, fix, pts);
@@ -728,9 +730,10 @@ int so_solve(void *h, double tol, int max_cycles, int smoother, int bottom, int 
     return 0;
 }
 
-int so_set_cycle(void *h, int v_down, int v_up, int bottom_sweeps) {
+int so_set_cycle(void *h, int v_down, int v_up, int bottom_sweeps, int grow) {
     H(h)->v_down = v_down;
     H(h)->v_up = v_up;
     H(h)->bottom_sweeps = bottom_sweeps;
+    H(h)->grow = grow;
     return 0;
 }

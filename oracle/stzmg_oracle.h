@@ -42,7 +42,7 @@ int so_vcycle(void *h, int smoother, int bottom);
 int so_residual(void *h, int l, double *out, double *sq);
 int so_solve(void *h, double tol, int max_cycles, int smoother, int bottom, int *cycles,
              double *hist);
-int so_set_cycle(void *h, int v_down, int v_up, int bottom_sweeps);
+int so_set_cycle(void *h, int v_down, int v_up, int bottom_sweeps, int grow);
 
 #ifdef __cplusplus
 }

@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <vector>
@@ -71,7 +73,7 @@ struct Level {
     T *coef = nullptr, *dinv = nullptr;             // dense levels
 };
 
-constexpr int kMaxLev = 16;
+constexpr int kMaxLev = kMaxLevels;
 
 }  // namespace
 
@@ -106,6 +108,11 @@ struct stz_mg_handle_s {
     double bnorm = -1.0;
     bool setup_done = false;
     cudaGraphExec_t gx64 = nullptr, gx32 = nullptr;
+    long long graph_kernels64 = 0, graph_kernels32 = 0;   // kernel nodes per captured V-cycle
+    // persistent cluster tail: levels tail_lo..nlev-2 (tail_lo < 0: none)
+    int tail_lo = -1, tail_cluster = 0, tail_cap_planes = 0;
+    int stat_cycles = 0, stat_residuals = 0;
+    long long stat_launches = 0;
     std::vector<void *> allocs;
 
     template <typename T>
@@ -308,12 +315,12 @@ void build_bottom(stz_mg_handle h) {
     {
         double *dcoef = nullptr;
         const double *src = nullptr;
-        if (lb == 0 && h->top_kind != OP_DENSE) {
+        if (h->op64[lb].kind != OP_DENSE) {
             dcoef = h->alloc<double>(243 * (size_t)g.npad);
-            launch_expand_dense(h->op64[0], g, dcoef, h->st);
+            launch_expand_dense(h->op64[lb], g, dcoef, h->st);
             src = dcoef;
         } else {
-            src = lb == 0 ? h->top_coef64 : h->L64[lb].coef;
+            src = h->op64[lb].dop.coef;
         }
         double *nat = staging(h, 243 * N);
         launch_coef_cb_to_nat(g, src, nat, h->st);
@@ -354,47 +361,68 @@ void build_bottom(stz_mg_handle h) {
                                 for (int c = 0; c < 3; c++) M[(3 * p + a) * nr + 3 * q + c] += blk[3 * a + c];
                         }
             }
-    // Gauss-Jordan inverse with partial pivoting, FP64.
-    std::vector<double> inv((size_t)nr * nr, 0.0);
-    for (int i = 0; i < nr; i++) inv[(size_t)i * nr + i] = 1.0;
-    for (int c = 0; c < nr; c++) {
-        int pv = c;
-        double best = std::fabs(M[(size_t)c * nr + c]);
-        for (int r = c + 1; r < nr; r++)
-            if (std::fabs(M[(size_t)r * nr + c]) > best) { best = std::fabs(M[(size_t)r * nr + c]); pv = r; }
-        if (!(best > 0) || !std::isfinite(best)) fail(STZ_MG_ERR_SINGULAR, "bottom-level matrix is singular");
-        if (pv != c)
-            for (int q = 0; q < nr; q++) {
-                std::swap(M[(size_t)c * nr + q], M[(size_t)pv * nr + q]);
-                std::swap(inv[(size_t)c * nr + q], inv[(size_t)pv * nr + q]);
-            }
-        const double piv = 1.0 / M[(size_t)c * nr + c];
-        for (int q = 0; q < nr; q++) { M[(size_t)c * nr + q] *= piv; inv[(size_t)c * nr + q] *= piv; }
-        for (int r = 0; r < nr; r++) {
-            if (r == c) continue;
-            const double f = M[(size_t)r * nr + c];
-            if (f == 0.0) continue;
-            for (int q = 0; q < nr; q++) {
-                M[(size_t)r * nr + q] -= f * M[(size_t)c * nr + q];
-                inv[(size_t)r * nr + q] -= f * inv[(size_t)c * nr + q];
-            }
-        }
+    // Gauss-Jordan inverse with partial pivoting, FP64, on the device.
+    std::vector<double> aug((size_t)nr * 2 * nr, 0.0);
+    for (int r = 0; r < nr; r++) {
+        std::memcpy(&aug[(size_t)r * 2 * nr], &M[(size_t)r * nr], nr * sizeof(double));
+        aug[(size_t)r * 2 * nr + nr + r] = 1.0;
     }
-    std::vector<double> invT((size_t)nr * nr);
-    for (int r = 0; r < nr; r++)
-        for (int c = 0; c < nr; c++) invT[(size_t)c * nr + r] = inv[(size_t)r * nr + c];
+    double *daug = h->alloc<double>(aug.size());
+    double *dcol = h->alloc<double>(nr);
+    int *dpiv = h->alloc<int>(1);
+    h->release(h->ainv_t);
+    h->ainv_t = h->alloc<double>((size_t)nr * nr);
+    CK(cudaMemcpyAsync(daug, aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+    launch_gauss_jordan(daug, nr, h->ainv_t, dpiv, dcol, h->dflag, h->st);
+    check_launch();
+    int singular = 0;
+    CK(cudaMemcpyAsync(&singular, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    sync(h);
+    h->release(daug);
+    h->release(dcol);
+    h->release(dpiv);
+    if (singular) fail(STZ_MG_ERR_SINGULAR, "bottom-level matrix is singular");
     std::vector<int> ns(N);
     for (int k = 0; k < g.o; k++)
         for (int j = 0; j < g.n; j++)
             for (int i = 0; i < g.m; i++) ns[i + (size_t)g.m * (j + (size_t)g.n * k)] = slot(g, i, j, k);
-    h->release(h->ainv_t);
     h->release(h->nat_slot);
-    h->ainv_t = h->alloc<double>((size_t)nr * nr);
     h->nat_slot = h->alloc<int>(N);
-    CK(cudaMemcpyAsync(h->ainv_t, invT.data(), invT.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync(h->nat_slot, ns.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->st));
     sync(h);
     h->nbot_rows = nr;
+}
+
+// Levels small enough for the persistent cluster kernels: the first coarse
+// level with at most kTailMaxNodes nodes down to the level above the bottom.
+constexpr size_t kTailMaxNodes = 300000;
+
+void choose_tail(stz_mg_handle h) {
+    h->tail_lo = -1;
+    h->tail_cluster = 0;
+    // off unless asked for: one 8-16 SM cluster is latency bound on these
+    // levels (see the design notes); kept for measurement
+    if (!std::getenv("STZ_MG_TAIL")) return;
+    const int L = h->nlev;
+    int lo = -1;
+    for (int l = 1; l <= L - 2; l++)
+        if (npts(h->geo[l]) <= kTailMaxNodes) { lo = l; break; }
+    if (lo < 0) return;
+    const bool mixed = h->d.precision == STZ_MG_MIXED;
+    const size_t tsz = mixed ? sizeof(float) : sizeof(double);
+    int cap = 0;
+    for (int l = lo; l <= L - 2; l++)
+        if (h->op64[l].kind == OP_PLANE) cap = std::max(cap, h->geo[l].o);
+    const int budget = 200 * 1024;
+    if ((size_t)cap * 252 * tsz > (size_t)budget) cap = (int)(budget / (252 * tsz));
+    const int smem = (int)(cap * 252 * tsz);
+    const int cl = mixed ? tail_cluster_size<float>(smem) : tail_cluster_size<double>(smem);
+    cudaGetLastError();
+    if (cl == 0) return;
+    h->tail_lo = lo;
+    h->tail_cluster = cl;
+    h->tail_cap_planes = cap;
 }
 
 void setup(stz_mg_handle h) {
@@ -419,34 +447,74 @@ void setup(stz_mg_handle h) {
     launch_top_bounds(h->geo[0], h->S[0], h->st);
     check_launch();
     CK(cudaMemsetAsync(h->dflag, 0, 2 * sizeof(int), h->st));
+    // A shared stencil on a grid periodic in x and y gives Galerkin operators
+    // that are the same on every node of an x-y plane: store and build one
+    // row per plane (exact, not an approximation).
+    const bool plane = h->top_kind == OP_CONST && h->geo[0].xp && h->geo[0].yp;
     for (int l = 1; l < h->nlev; l++) {
         const Geom &gf = h->geo[l - 1], &gc = h->geo[l];
+        const size_t rows = plane ? (size_t)gc.o : (size_t)gc.npad;
         Level<double> &C = h->L64[l];
-        if (!C.coef) {
-            C.coef = h->alloc<double>(243 * (size_t)gc.npad);
-            C.dinv = h->alloc<double>(9 * (size_t)gc.npad);
-        }
+        h->release(C.coef);
+        h->release(C.dinv);
+        C.coef = h->alloc<double>(243 * rows);
+        C.dinv = h->alloc<double>(9 * rows);
         launch_rat_bounds(gf, h->S[l - 1], gc, h->S[l], h->dflag + 1, h->st);
-        launch_rat(h->op64[l - 1], gf, gc, C.coef, h->st);
-        launch_dense_dinv<double>(gc, C.coef, C.dinv, h->dflag, h->st);
+        launch_rat(h->op64[l - 1], gf, gc, C.coef, plane, h->st);
+        if (plane) launch_plane_dinv<double>(gc.o, C.coef, C.dinv, h->dflag, h->st);
+        else launch_dense_dinv<double>(gc, C.coef, C.dinv, h->dflag, h->st);
         check_launch();
         h->op64[l] = LevelOp<double>{};
-        h->op64[l].kind = OP_DENSE;
-        h->op64[l].dop.coef = C.coef;
-        h->op64[l].dop.dinv = C.dinv;
+        int sparse = 0, sparse32 = 0;
+        if (plane) {
+            // The Galerkin operators of the constant elasticity stencil vanish on
+            // the entries outside coarse_entry() up to cancellation round-off.
+            // FP64 kernels skip them only when they are exactly zero; FP32
+            // kernels when they are below 1e-9 of the plane's largest entry
+            // (far below FP32 resolution).
+            std::vector<double> pc(243 * rows);
+            CK(cudaMemcpyAsync(pc.data(), C.coef, pc.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            sync(h);
+            double worst_rel = 0.0;
+            bool exact = true;
+            for (size_t k = 0; k < rows; k++) {
+                double amax = 0.0, dropped = 0.0;
+                for (int b = 0; b < 27; b++)
+                    for (int e = 0; e < 9; e++) {
+                        double v = std::fabs(pc[(9 * b + e) * rows + k]);
+                        amax = std::max(amax, v);
+                        if (!coarse_entry(b, e)) dropped = std::max(dropped, v);
+                    }
+                if (dropped != 0.0) exact = false;
+                if (amax > 0) worst_rel = std::max(worst_rel, dropped / amax);
+            }
+            sparse = exact;
+            sparse32 = worst_rel <= 1e-9;
+        }
+        if (plane) {
+            h->op64[l].kind = OP_PLANE;
+            h->op64[l].pop = PlaneOp<double>{C.coef, C.dinv, gc.o, sparse};
+        } else {
+            h->op64[l].kind = OP_DENSE;
+            h->op64[l].dop = DenseOp<double>{C.coef, C.dinv};
+        }
         if (mixed) {
             Level<float> &F = h->L32[l];
-            if (!F.coef) {
-                F.coef = h->alloc<float>(243 * (size_t)gc.npad);
-                F.dinv = h->alloc<float>(9 * (size_t)gc.npad);
-            }
-            launch_convert(C.coef, F.coef, 243 * (size_t)gc.npad, h->st);
-            launch_convert(C.dinv, F.dinv, 9 * (size_t)gc.npad, h->st);
+            h->release(F.coef);
+            h->release(F.dinv);
+            F.coef = h->alloc<float>(243 * rows);
+            F.dinv = h->alloc<float>(9 * rows);
+            launch_convert(C.coef, F.coef, 243 * rows, h->st);
+            launch_convert(C.dinv, F.dinv, 9 * rows, h->st);
             check_launch();
             h->op32[l] = LevelOp<float>{};
-            h->op32[l].kind = OP_DENSE;
-            h->op32[l].dop.coef = F.coef;
-            h->op32[l].dop.dinv = F.dinv;
+            if (plane) {
+                h->op32[l].kind = OP_PLANE;
+                h->op32[l].pop = PlaneOp<float>{F.coef, F.dinv, gc.o, sparse32};
+            } else {
+                h->op32[l].kind = OP_DENSE;
+                h->op32[l].dop = DenseOp<float>{F.coef, F.dinv};
+            }
         }
     }
     int flags[2] = {0, 0};
@@ -455,6 +523,7 @@ void setup(stz_mg_handle h) {
     if (flags[1]) fail(STZ_MG_ERR_UNSUPPORTED, "RAT box bounds out of range");
     if (flags[0]) fail(STZ_MG_ERR_SINGULAR, "singular or non-finite diagonal block on a coarse level");
     if (h->d.bottom == STZ_MG_BOTTOM_DIRECT) build_bottom(h);
+    choose_tail(h);
     h->setup_done = true;
 }
 
@@ -480,25 +549,58 @@ void bottom_solve(stz_mg_handle h, Hier<T> H) {
 // going down, then restriction (residual + (1/8)P^T, coarse x cleared); the
 // bottom is solved; going up, interpolation then v_up+i-1 sweeps.
 template <typename T>
+TailDesc<T> tail_desc(stz_mg_handle h, Hier<T> H) {
+    TailDesc<T> d{};
+    d.lo = h->tail_lo;
+    d.hi = h->nlev - 2;
+    d.v_down = h->d.v_down;
+    d.v_up = h->d.v_up;
+    d.growth = h->d.sweep_growth;
+    d.cap_planes = h->tail_cap_planes;
+    for (int l = 0; l < h->nlev; l++) {
+        TailLev<T> &t = d.L[l];
+        t.g = h->geo[l];
+        t.kind = H.op[l].kind;
+        if (t.kind == OP_PLANE) {
+            t.coef = H.op[l].pop.coef; t.dinv = H.op[l].pop.dinv; t.O = H.op[l].pop.O; t.sparse = H.op[l].pop.sparse;
+        } else {
+            t.coef = H.op[l].dop.coef; t.dinv = H.op[l].dop.dinv; t.O = 0; t.sparse = 0;
+        }
+        t.x = H.L[l].x; t.r = H.L[l].r; t.res = H.L[l].res;
+    }
+    return d;
+}
+
+// multigrid::v_cycle (multigrid.cc:253-297) with the levels below the tail
+// threshold run by the two persistent cluster kernels.
+template <typename T>
 void enqueue_vcycle(stz_mg_handle h, Hier<T> H) {
     const int L = h->nlev;
-    for (int i = 0; i < L - 1; i++) {
+    const int lo = h->tail_lo >= 0 ? h->tail_lo : L - 1;
+    for (int i = 0; i < lo; i++) {
         const Geom &g = h->geo[i];
-        for (int s = 0; s < h->d.v_down + i; s++) launch_gs_sweep<T>(H.op[i], g, H.L[i].r, H.L[i].x, h->st);
+        for (int s = 0; s < h->d.v_down + (h->d.sweep_growth ? i : 0); s++)
+            launch_gs_sweep<T>(H.op[i], g, H.L[i].r, H.L[i].x, h->st);
         launch_residual<T, T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, nullptr, nullptr, h->st);
         launch_restriction<T>(g, h->geo[i + 1], H.L[i].res, H.L[i + 1].r, h->st);
         CK(cudaMemsetAsync(H.L[i + 1].x, 0, 3 * (size_t)h->geo[i + 1].npad * sizeof(T), h->st));
     }
+    TailDesc<T> td{};
+    if (h->tail_lo >= 0) {
+        td = tail_desc<T>(h, H);
+        CK(launch_tail_down<T>(td, h->tail_cluster, h->st));
+    }
     bottom_solve<T>(h, H);
-    for (int i = L - 1; i > 0; i--) {
+    if (h->tail_lo >= 0) CK(launch_tail_up<T>(td, h->tail_cluster, h->st));
+    for (int i = lo; i > 0; i--) {
         launch_interpolation<T>(h->geo[i - 1], h->geo[i], H.L[i].x, H.L[i - 1].x, h->st);
-        for (int s = 0; s < h->d.v_up + i - 1; s++)
+        for (int s = 0; s < h->d.v_up + (h->d.sweep_growth ? i - 1 : 0); s++)
             launch_gs_sweep<T>(H.op[i - 1], h->geo[i - 1], H.L[i - 1].r, H.L[i - 1].x, h->st);
     }
 }
 
 template <typename T>
-cudaGraphExec_t capture_vcycle(stz_mg_handle h, Hier<T> H) {
+cudaGraphExec_t capture_vcycle(stz_mg_handle h, Hier<T> H, long long *kernel_nodes) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     try {
@@ -508,6 +610,17 @@ cudaGraphExec_t capture_vcycle(stz_mg_handle h, Hier<T> H) {
         throw;
     }
     CK(cudaStreamEndCapture(h->st, &graph));
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+    long long nk = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) nk++;
+    }
+    *kernel_nodes = nk;
     cudaGraphExec_t ex;
     CK(cudaGraphInstantiate(&ex, graph, 0));
     CK(cudaGraphDestroy(graph));
@@ -518,13 +631,17 @@ Hier<double> hier64(stz_mg_handle h) { return Hier<double>{h->L64, h->op64}; }
 Hier<float> hier32(stz_mg_handle h) { return Hier<float>{h->L32, h->op32}; }
 
 void run_vcycle64(stz_mg_handle h, int count) {
-    if (!h->gx64) h->gx64 = capture_vcycle<double>(h, hier64(h));
+    if (!h->gx64) h->gx64 = capture_vcycle<double>(h, hier64(h), &h->graph_kernels64);
     for (int c = 0; c < count; c++) CK(cudaGraphLaunch(h->gx64, h->st));
+    h->stat_cycles += count;
+    h->stat_launches += count * h->graph_kernels64;
 }
 
 void run_vcycle32(stz_mg_handle h, int count) {
-    if (!h->gx32) h->gx32 = capture_vcycle<float>(h, hier32(h));
+    if (!h->gx32) h->gx32 = capture_vcycle<float>(h, hier32(h), &h->graph_kernels32);
     for (int c = 0; c < count; c++) CK(cudaGraphLaunch(h->gx32, h->st));
+    h->stat_cycles += count;
+    h->stat_launches += count * h->graph_kernels32;
 }
 
 // |b - A x|^2 of the top FP64 level; when r32 is non-null the residual is
@@ -537,6 +654,8 @@ double top_residual_sq(stz_mg_handle h, float *r32) {
         launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial,
                                         h->dscal, h->st);
     check_launch();
+    h->stat_residuals++;
+    h->stat_launches += 2;   // residual + partial-sum reduction
     CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     sync(h);
     double v = h->hscal[0];
@@ -571,10 +690,13 @@ void mixed_step(stz_mg_handle h, int k) {
     run_vcycle32(h, k);
     launch_add_correction(h->L64[0].x, h->L32[0].x, n3, h->st);
     check_launch();
+    h->stat_launches += 1;
 }
 
 void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double *relres_out) {
     need_setup(h);
+    h->stat_cycles = h->stat_residuals = 0;
+    h->stat_launches = 0;
     const double bn = rhs_norm(h);
     const double target = tol * (bn > 0 ? bn : 1.0);
     int cycles = 0;
@@ -593,18 +715,22 @@ void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double 
         // the tolerance.
         rsq = top_residual_sq(h, h->L32[0].r);
         double rn = std::sqrt(rsq), rho = 0.2;
-        int k = 3;
+        int k = 6;
+        const bool trace = std::getenv("STZ_MG_TRACE") != nullptr;
         while (rn > target && cycles < max_cycles) {
             k = std::max(1, std::min(k, max_cycles - cycles));
             mixed_step(h, k);
             cycles += k;
             rsq = top_residual_sq(h, h->L32[0].r);
             double rn_new = std::sqrt(rsq);
+            if (trace) fprintf(stderr, "stz_mg mixed: %d cycles, |r|/|b| %.3e -> %.3e\n", k, rn / bn, rn_new / bn);
             double gain = rn_new / rn;
             if (gain > 0 && gain < 1) rho = std::min(0.9, std::max(1e-3, std::pow(gain, 1.0 / k)));
             else rho = 0.9;
             rn = rn_new;
-            double want = std::max(target / rn, 2e-6);
+            // aim a decade below the tolerance when it is within reach, so the
+            // last step does not fall just short (each step costs an FP64 residual)
+            double want = std::max(0.1 * target / rn, 1e-6);
             k = (int)std::ceil(std::log(want) / std::log(rho) - 1e-9);
             k = std::max(1, std::min(k, 12));
         }
@@ -627,9 +753,10 @@ void stz_mg_desc_default(stz_mg_desc *d) {
     d->precision = STZ_MG_FP64;
     d->v_down = 2;
     d->v_up = 2;
-    d->max_coarse = 16;
+    d->max_coarse = 1024;
     d->bottom = STZ_MG_BOTTOM_DIRECT;
     d->bottom_sweeps = 24;
+    d->sweep_growth = 1;
     d->device = 0;
     d->stream = nullptr;
 }
@@ -810,6 +937,33 @@ int stz_mg_get_x(stz_mg_handle h, double *x, int where) {
     });
 }
 
+int stz_mg_get_rhs(stz_mg_handle h, double *r, int where) {
+    if (!h || !r) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const size_t n = 3 * npts(g);
+        double *d = where == STZ_MG_DEVICE ? r : staging(h, n);
+        launch_cb_to_nat<double>(g, h->L64[0].r, d, h->st);
+        check_launch();
+        if (where != STZ_MG_DEVICE) CK(cudaMemcpyAsync(r, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_set_rhs_divergence(stz_mg_handle h, const double *eps, double dx, double dy, double dz, int where) {
+    if (!h || !eps) return set_error(STZ_MG_ERR_ARG, "null argument");
+    if (!(dx > 0 && dy > 0 && dz > 0)) return set_error(STZ_MG_ERR_ARG, "bad spacing");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const size_t ncells = (size_t)(g.xp ? g.m : g.m - 1) * (g.yp ? g.n : g.n - 1) * (g.zp ? g.o : g.o - 1);
+        const double *src = to_device(h, eps, 6 * ncells, where);
+        launch_rhs_divergence(g, src, dx, dy, dz, h->L64[0].r, h->st);
+        check_launch();
+        h->bnorm = -1.0;
+        sync(h);
+    });
+}
+
 int stz_mg_vcycle(stz_mg_handle h) {
     if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
     return guarded(h, [&] {
@@ -828,6 +982,14 @@ int stz_mg_solve(stz_mg_handle h, double rel_tol, int max_cycles, int *cycles, d
     if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
     if (!(rel_tol > 0) || max_cycles < 0) return set_error(STZ_MG_ERR_ARG, "bad tolerance or cycle cap");
     return guarded(h, [&] { solve(h, rel_tol, max_cycles, cycles, relres); });
+}
+
+int stz_mg_solve_stats(stz_mg_handle h, int *vcycles, int *residuals, long long *kernel_launches) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    if (vcycles) *vcycles = h->stat_cycles;
+    if (residuals) *residuals = h->stat_residuals;
+    if (kernel_launches) *kernel_launches = h->stat_launches;
+    return STZ_MG_OK;
 }
 
 int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm) {
@@ -887,12 +1049,12 @@ int stz_mg_level_operator(stz_mg_handle h, int level, double *A, int *S) {
         if (A) {
             double *dcoef = nullptr;
             const double *src;
-            if (level == 0 && h->top_kind != OP_DENSE) {
+            if (h->op64[level].kind != OP_DENSE) {
                 dcoef = h->alloc<double>(243 * (size_t)g.npad);
-                launch_expand_dense(h->op64[0], g, dcoef, h->st);
+                launch_expand_dense(h->op64[level], g, dcoef, h->st);
                 src = dcoef;
             } else {
-                src = level == 0 ? h->top_coef64 : h->L64[level].coef;
+                src = h->op64[level].dop.coef;
             }
             double *nat = staging(h, 243 * N);
             launch_coef_cb_to_nat(g, src, nat, h->st);
@@ -997,6 +1159,84 @@ int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq
         }
         sync(h);
         if (sumsq) *sumsq = h->hscal[0];
+    });
+}
+
+
+int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
+                       double *work_per_launch) {
+    if (!h || reps < 1) return set_error(STZ_MG_ERR_ARG, "bad argument");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        const bool mixed = h->d.precision == STZ_MG_MIXED;
+        const Geom &g = h->geo[level];
+        const double npts_l = (double)npts(g);
+        const double s = mixed ? 4.0 : 8.0;
+        auto coef_bytes = [&](int l) -> double {   // coefficient bytes per node of level l
+            const LevelOp<double> &op = h->op64[l];
+            if (op.kind == OP_DENSE) return (243 + 9) * s;
+            if (op.kind == OP_LAME) return 2 * s;
+            if (op.kind == OP_PLANE) return (243 + 9) * s * h->geo[l].o / (double)npts(h->geo[l]);
+            return 0.0;
+        };
+        std::function<void()> launch;
+        double work = 0;
+        switch (kernel) {
+            case STZ_MG_K_GS_COLOUR:
+                // a full 8-colour sweep reads x and r and writes x once per node
+                work = (9 * s + coef_bytes(level)) * npts_l / 8;
+                if (mixed) launch = [&] { launch_gs_colour<float>(h->op32[level], g, 0, h->L32[level].r, h->L32[level].x, h->st); };
+                else launch = [&] { launch_gs_colour<double>(h->op64[level], g, 0, h->L64[level].r, h->L64[level].x, h->st); };
+                break;
+            case STZ_MG_K_RESIDUAL:
+                work = (9 * s + coef_bytes(level)) * npts_l;
+                if (mixed) launch = [&] { launch_residual<float, float>(h->op32[level], g, h->L32[level].r, h->L32[level].x, h->L32[level].res, nullptr, nullptr, h->st); };
+                else launch = [&] { launch_residual<double, double>(h->op64[level], g, h->L64[level].r, h->L64[level].x, h->L64[level].res, nullptr, nullptr, h->st); };
+                break;
+            case STZ_MG_K_RESTRICT: {
+                if (level < 1) fail(STZ_MG_ERR_ARG, "restriction target must be a coarse level");
+                const Geom &gf = h->geo[level - 1];
+                work = 3 * s * ((double)npts(gf) + npts_l);
+                if (mixed) launch = [&] { launch_restriction<float>(gf, g, h->L32[level - 1].res, h->L32[level].r, h->st); };
+                else launch = [&] { launch_restriction<double>(gf, g, h->L64[level - 1].res, h->L64[level].r, h->st); };
+                break;
+            }
+            case STZ_MG_K_INTERP: {
+                if (level < 1) fail(STZ_MG_ERR_ARG, "interpolation source must be a coarse level");
+                const Geom &gf = h->geo[level - 1];
+                work = 6 * s * (double)npts(gf) + 3 * s * npts_l;
+                if (mixed) launch = [&] { launch_interpolation<float>(gf, g, h->L32[level].x, h->L32[level - 1].x, h->st); };
+                else launch = [&] { launch_interpolation<double>(gf, g, h->L64[level].x, h->L64[level - 1].x, h->st); };
+                break;
+            }
+            case STZ_MG_K_RESIDUAL64: {
+                if (level != 0) fail(STZ_MG_ERR_ARG, "the FP64 residual is a top-level kernel");
+                // FP64 flops of r = b - A x with the elasticity stencil: 6 faces x 3 + 12 edges x 2
+                // + centre 9 multiply-adds per node (a dense stencil: 243)
+                const LevelOp<double> &op = h->op64[0];
+                double fma = op.kind == OP_CONST && op.cop.elastic ? 51 : op.kind == OP_LAME ? 51 : 243;
+                work = 2 * fma * npts_l;
+                if (mixed) launch = [&] { launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].r, h->partial, h->dscal, h->st); };
+                else launch = [&] { launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial, h->dscal, h->st); };
+                break;
+            }
+            default: fail(STZ_MG_ERR_ARG, "unknown kernel id %d", kernel);
+        }
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        for (int w = 0; w < 3; w++) launch();
+        CK(cudaEventRecord(e0, h->st));
+        for (int r = 0; r < reps; r++) launch();
+        CK(cudaEventRecord(e1, h->st));
+        sync(h);
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ms_per_launch) *ms_per_launch = ms / reps;
+        if (work_per_launch) *work_per_launch = work;
     });
 }
 

@@ -71,6 +71,29 @@ __device__ inline NbrOffsets nbr_offsets(const Geom &g, int i, int j, int k) {
     return t;
 }
 
+// Neighbour offsets from sub-grid coordinates without divisions: node
+// (2I+a, 2J+b, 2K+c); same result as nbr_offsets(g, 2I+a, 2J+b, 2K+c).
+__device__ inline void dim_offsets(int I, int a, int n, int N2, int prd, int pstride, int istride, int *o) {
+    const int BAD = INT32_MIN / 4;
+    o[1] = a * pstride + I * istride;
+    if (n == 1) {   // a single periodic node is its own neighbour
+        o[0] = o[2] = prd ? o[1] : BAD;
+        return;
+    }
+    if (a) o[0] = I * istride;
+    else o[0] = I > 0 ? pstride + (I - 1) * istride : (prd ? pstride + (N2 - 1) * istride : BAD);
+    if (2 * I + a + 1 < n) o[2] = a ? (I + 1) * istride : pstride + I * istride;
+    else o[2] = prd ? 0 : BAD;
+}
+
+__device__ inline NbrOffsets nbr_offsets_sub(const Geom &g, int I, int J, int K, int a, int b, int c) {
+    NbrOffsets t;
+    dim_offsets(I, a, g.m, g.M2, g.xp, g.S, 1, t.ox);
+    dim_offsets(J, b, g.n, g.N2, g.yp, 2 * g.S, g.M2, t.oy);
+    dim_offsets(K, c, g.o, g.O2, g.zp, 4 * g.S, g.M2 * g.N2, t.oz);
+    return t;
+}
+
 // Node coordinates of thread t within colour q's sub-grid; false for an
 // unused slot.
 __device__ inline bool colour_node(const Geom &g, int q, int t, int &i, int &j, int &k) {
@@ -80,6 +103,17 @@ __device__ inline bool colour_node(const Geom &g, int q, int t, int &i, int &j, 
     j = 2 * J + ((q >> 1) & 1);
     k = 2 * K + ((q >> 2) & 1);
     return i < g.m && j < g.n && k < g.o;
+}
+
+// Thread mapping of kernels that visit every node: a block of 8 warps covers
+// the same 32 consecutive sub-grid slots in all 8 colours (warp w = colour w),
+// i.e. a compact 64x2x2 region of the level, so neighbour reads are shared in
+// L1 across the colours; within a warp the slots stay consecutive (coalesced).
+// Launch with blockDim 256 and ceil(S/32) blocks.  Returns the slot or -1.
+__device__ inline int interleaved_slot(const Geom &g) {
+    const int q = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + (threadIdx.x & 31);
+    return t < g.S ? q * g.S + t : -1;
 }
 
 // Node coordinates of slot p (any colour).
@@ -94,8 +128,10 @@ __host__ __device__ inline bool is_interior(const Geom &g, int i, int j, int k) 
            (g.zp || (k != 0 && k != g.o - 1));
 }
 
-// Operator kinds.
-enum OpKind { OP_CONST = 0, OP_LAME = 1, OP_DENSE = 2 };
+// Operator kinds.  OP_PLANE is a coarse operator that does not vary across
+// an x-y plane (the Galerkin operators of a shared stencil on a grid periodic
+// in x and y): one row of 27 blocks per z-plane.
+enum OpKind { OP_CONST = 0, OP_LAME = 1, OP_DENSE = 2, OP_PLANE = 3 };
 
 // Shared constant stencil (external_ptr path): interior nodes use a[27][9],
 // Dirichlet nodes use fix; inverses of both centre blocks precomputed.
@@ -123,6 +159,19 @@ template <typename T>
 struct DenseOp {
     const T *coef;  // 243 * npad
     const T *dinv;  // 9 * npad, inverse of the centre block
+};
+
+// Plane-invariant coefficients: entry e of block b on plane k at
+// coef[(9*b + e) * O + k]; inverse centre blocks at dinv[e * O + k].
+// `sparse` marks operators whose entry (r,c) of the block at offset d is zero
+// unless r == c or both d_r and d_c are non-zero (the structure of the
+// Galerkin operators of the constant elasticity stencil: 153 of 243 entries).
+template <typename T>
+struct PlaneOp {
+    const T *coef;
+    const T *dinv;
+    int O;
+    int sparse;
 };
 
 template <typename T>

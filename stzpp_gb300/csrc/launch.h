@@ -7,6 +7,8 @@
 
 namespace stzmg {
 
+constexpr int kMaxLevels = 16;
+
 // One level's operator as the kernels see it.
 template <typename T>
 struct LevelOp {
@@ -14,6 +16,7 @@ struct LevelOp {
     ConstOp<T> cop;
     LameOp<T> lop;
     DenseOp<T> dop;
+    PlaneOp<T> pop;
 };
 
 // smooth.cu
@@ -48,16 +51,53 @@ void launch_coef_cb_to_nat(const Geom &g, const double *cb, double *nat, cudaStr
 void launch_convert(const double *src, float *dst, size_t n, cudaStream_t st);
 // x64 += e32 over n elements
 void launch_add_correction(double *x, const float *e, size_t n, cudaStream_t st);
-// x = Ainv r on the bottom level: Ainv is (3N)^2 column-major (Ainv_T[col*3N+row]),
-// nat_slot maps natural node index -> slot.
+// x = Ainv r on the bottom level: Ainv is (3N)^2 row-major in natural node
+// order (3 rows per node); nat_slot maps natural node index -> slot.
 template <typename T>
 void launch_bottom_direct(int nrow, const double *ainv_t, const int *nat_slot, int npad, const T *r, T *x,
                           cudaStream_t st);
 void launch_scale(double *v, double s, size_t n, cudaStream_t st);
+// inverse of the n x n matrix in the left half of the augmented n x 2n matrix
+// [M | I] (row-major, overwritten) into inv (row-major); bad[0] set when singular
+void launch_gauss_jordan(double *aug, int n, double *inv, int *piv, double *col, int *bad, cudaStream_t st);
+
+// field.cu
+// r (colour-blocked, 3 x npad) = node divergence of the cell tensor field eps
+void launch_rhs_divergence(const Geom &g, const double *eps, double dx, double dy, double dz, double *r,
+                           cudaStream_t st);
+
+// tail.cu: persistent cluster kernels for the small levels lo..hi (hi+1 is
+// the bottom level).  Levels must be OP_PLANE or OP_DENSE.
+constexpr int kTailThreads = 1024;
+template <typename T>
+struct TailLev {
+    Geom g;
+    int kind;
+    const T *coef, *dinv;
+    int O, sparse;
+    T *x, *r, *res;
+};
+template <typename T>
+struct TailDesc {
+    int lo, hi, v_down, v_up, growth, cap_planes;
+    TailLev<T> L[kMaxLevels];
+};
+template <typename T>
+cudaError_t launch_tail_down(const TailDesc<T> &d, int cluster, cudaStream_t st);
+template <typename T>
+cudaError_t launch_tail_up(const TailDesc<T> &d, int cluster, cudaStream_t st);
+// cluster size (16 or 8) the device can run with this shared memory, or 0
+template <typename T>
+int tail_cluster_size(int smem_bytes);
 
 // rat.cu
-// Galerkin coarse operator A_c = (1/8) P^T A P into a dense SoA field (243 x npad_c).
-void launch_rat(const LevelOp<double> &fine, const Geom &gf, const Geom &gc, double *coef_c, cudaStream_t st);
+// Galerkin coarse operator A_c = (1/8) P^T A P into a dense SoA field (243 x npad_c),
+// or, when plane is set, into plane storage (243 x o_c) from the column i = j = 0.
+void launch_rat(const LevelOp<double> &fine, const Geom &gf, const Geom &gc, double *coef_c, bool plane,
+                cudaStream_t st);
+// inverse centre blocks of plane storage
+template <typename T>
+void launch_plane_dinv(int O, const T *coef, T *dinv, int *bad, cudaStream_t st);
 // dense 27-block SoA copy of any operator (top level export)
 void launch_expand_dense(const LevelOp<double> &op, const Geom &g, double *coef, cudaStream_t st);
 // inverse of every centre block; bad[0] set to 1 on a singular/non-finite block

@@ -28,11 +28,20 @@ __host__ __device__ constexpr bool elastic_entry(int b, int e) {
          : false;
 }
 
-template <typename T>
+// COH: the field is written by other blocks of the same launch (the
+// persistent small-level kernel), so read it through L2 (ld.global.cg), not
+// from a possibly stale L1 line.
+template <typename T, bool COH = false>
 __device__ inline void load3(const T *__restrict__ f, int npad, int s, T *v) {
-    v[0] = f[s];
-    v[1] = f[s + npad];
-    v[2] = f[s + 2 * npad];
+    if (COH) {
+        v[0] = __ldcg(f + s);
+        v[1] = __ldcg(f + s + npad);
+        v[2] = __ldcg(f + s + 2 * npad);
+    } else {
+        v[0] = f[s];
+        v[1] = f[s + npad];
+        v[2] = f[s + 2 * npad];
+    }
 }
 
 // ---------------------------------------------------------------- constant
@@ -40,19 +49,31 @@ __device__ inline void load3(const T *__restrict__ f, int npad, int s, T *v) {
 template <typename T, bool ELASTIC, bool WITH_CENTRE>
 __device__ inline void const_row(const ConstOp<T> &op, const Geom &g, const NbrOffsets &t,
                                  const T *__restrict__ x, T *acc) {
+    // neighbour components first (only those the stencil uses), then arithmetic
+    T v[27][3];
 #pragma unroll
     for (int b = 0; b < 27; b++) {
         if (b == 13 && !WITH_CENTRE) continue;
         if (ELASTIC && nnz_axes(b) == 3) continue;
         int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
-        T v[3];
-        load3(x, g.npad, s, v);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            bool used = !ELASTIC || b == 13;
+#pragma unroll
+            for (int r = 0; r < 3; r++) used = used || elastic_entry(b, 3 * r + c);
+            v[b][c] = used ? x[s + c * g.npad] : T(0);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < 27; b++) {
+        if (b == 13 && !WITH_CENTRE) continue;
+        if (ELASTIC && nnz_axes(b) == 3) continue;
         if (ELASTIC && b != 13) {
 #pragma unroll
             for (int e = 0; e < 9; e++)
-                if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[e % 3];
+                if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[b][e % 3];
         } else {
-            matvec_sub(op.a[b], v, acc);
+            matvec_sub(op.a[b], v[b], acc);
         }
     }
 }
@@ -156,7 +177,7 @@ __device__ inline T lame_fix(const LameOp<T> &op, int p) {
 }
 
 // ---------------------------------------------------------------- dense
-template <typename T, bool WITH_CENTRE>
+template <typename T, bool WITH_CENTRE, bool COH = false>
 __device__ inline void dense_row(const DenseOp<T> &op, const Geom &g, const NbrOffsets &t, int p,
                                  const T *__restrict__ x, T *acc) {
     const size_t np = (size_t)g.npad;
@@ -166,11 +187,60 @@ __device__ inline void dense_row(const DenseOp<T> &op, const Geom &g, const NbrO
         int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
         if (s < 0) continue;   // outside a non-periodic grid: coefficients are zero there
         T v[3], a[9];
-        load3(x, g.npad, s, v);
+        load3<T, COH>(x, g.npad, s, v);
         const T *cb = op.coef + (size_t)(9 * b) * np + p;
 #pragma unroll
         for (int e = 0; e < 9; e++) a[e] = __ldg(cb + (size_t)e * np);
         matvec_sub(a, v, acc);
+    }
+}
+
+// ---------------------------------------------------------------- plane
+// Structural non-zeros of the coarse elasticity operators: entry (r,c) of the
+// block at offset d can be non-zero only if r == c or d_r, d_c are both non-zero.
+__host__ __device__ constexpr bool coarse_entry(int b, int e) {
+    return (e / 3 == e % 3) ||
+           ((e / 3 == 0 ? bdx(b) : e / 3 == 1 ? bdy(b) : bdz(b)) != 0 &&
+            (e % 3 == 0 ? bdx(b) : e % 3 == 1 ? bdy(b) : bdz(b)) != 0);
+}
+
+// acc -= sum_b A_b x_b with entry e of block b read from cf[(9b + e) * stride]
+// (shared memory with stride 1, or plane storage in global memory).
+template <typename T, bool SPARSE, bool WITH_CENTRE, bool COH = false>
+__device__ inline void plane_row_coef(const T *cf, int stride, const Geom &g, const NbrOffsets &t,
+                                      const T *__restrict__ x, T *acc) {
+    if (sizeof(T) == 8) {
+        // FP64: arithmetic bound; load each neighbour right before its block
+#pragma unroll
+        for (int b = 0; b < 27; b++) {
+            if (b == 13 && !WITH_CENTRE) continue;
+            int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
+            if (s < 0) continue;
+            T v[3];
+            load3<T, COH>(x, g.npad, s, v);
+#pragma unroll
+            for (int e = 0; e < 9; e++)
+                if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[(9 * b + e) * stride] * v[e % 3];
+        }
+        return;
+    }
+    // FP32: all neighbour loads are issued before the arithmetic so that they
+    // are in flight together (one memory latency per node, not one per block)
+    T v[27][3];
+#pragma unroll
+    for (int b = 0; b < 27; b++) {
+        if (b == 13 && !WITH_CENTRE) continue;
+        int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
+        const int sc = s < 0 ? 0 : s;
+        load3<T, COH>(x, g.npad, sc, v[b]);
+        if (s < 0) v[b][0] = v[b][1] = v[b][2] = T(0);
+    }
+#pragma unroll
+    for (int b = 0; b < 27; b++) {
+        if (b == 13 && !WITH_CENTRE) continue;
+#pragma unroll
+        for (int e = 0; e < 9; e++)
+            if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[(9 * b + e) * stride] * v[b][e % 3];
     }
 }
 

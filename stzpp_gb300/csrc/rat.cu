@@ -72,18 +72,27 @@ __device__ inline void fine_block(const LevelOp<double> &op, const Geom &g, int 
             a[3 * r + c] = -op.lop.dt * ((sgn * (lam_r + mu_c)) / den);
             a[3 * c + r] = -op.lop.dt * ((sgn * (lam_c + mu_r)) / den);
         }
+    } else if (KIND == OP_PLANE) {
+        const int k = fs;   // callers pass the plane index for plane operators
+        for (int e = 0; e < 9; e++) a[e] = op.pop.coef[(9 * b + e) * op.pop.O + k];
     } else {
         const size_t np = (size_t)g.npad;
         for (int e = 0; e < 9; e++) a[e] = op.dop.coef[(size_t)(9 * b + e) * np + fs];
     }
 }
 
-template <int KIND>
+template <int KIND, bool OUT_PLANE>
 __global__ void __launch_bounds__(kRB) rat_kernel(Geom gf, Geom gc, const __grid_constant__ LevelOp<double> op,
                                                   double *__restrict__ coef_c) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x, off = blockIdx.y;
     int I, J, K;
-    if (p >= gc.npad || !slot_node(gc, p, I, J, K)) return;
+    if (OUT_PLANE) {
+        // one coarse node per plane: the column i = j = 0
+        if (p >= gc.o) return;
+        I = 0; J = 0; K = p;
+    } else if (p >= gc.npad || !slot_node(gc, p, I, J, K)) {
+        return;
+    }
     const int ox = bdx(off), oy = bdy(off), oz = bdz(off);
     const int TI = I + ox, TJ = J + oy, TK = K + oz;   // target coarse node (unwrapped)
     int tlo[3], thi[3], tc[3];
@@ -107,8 +116,8 @@ __global__ void __launch_bounds__(kRB) rat_kernel(Geom gf, Geom gc, const __grid
             for (int fx = slo[0]; fx < shi[0]; fx++) {
                 const double wf = fx == sc[0] ? wfy : 0.5 * wfy;
                 const int fxw = wrapd(fx, gf.m);
-                const int fs = slot(gf, fxw, fyw, fzw);
-                const bool interior = KIND == OP_DENSE ? true : is_interior(gf, fxw, fyw, fzw);
+                const int fs = KIND == OP_PLANE ? fzw : slot(gf, fxw, fyw, fzw);
+                const bool interior = (KIND == OP_DENSE || KIND == OP_PLANE) ? true : is_interior(gf, fxw, fyw, fzw);
                 // box of f: [-1,1]^3 for interior rows (and every dense row), centre only otherwise
                 const int r0 = interior ? -1 : 0, r1 = interior ? 1 : 0;
                 LameRow<double> L;
@@ -140,9 +149,19 @@ __global__ void __launch_bounds__(kRB) rat_kernel(Geom gf, Geom gc, const __grid
             }
         }
     }
-    const size_t np = (size_t)gc.npad;
+    const size_t np = OUT_PLANE ? (size_t)gc.o : (size_t)gc.npad;
 #pragma unroll
     for (int e = 0; e < 9; e++) coef_c[(size_t)(9 * off + e) * np + p] = acc[e];
+}
+
+template <typename T>
+__global__ void plane_dinv_kernel(int O, const T *__restrict__ coef, T *__restrict__ dinv, int *bad) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= O) return;
+    T a[9], inv[9];
+    for (int e = 0; e < 9; e++) a[e] = coef[(9 * 13 + e) * O + k];
+    if (!inverse3(a, inv)) atomicExch(bad, 1);
+    for (int e = 0; e < 9; e++) dinv[e * O + k] = inv[e];
 }
 
 template <typename T>
@@ -246,7 +265,7 @@ __global__ void expand_dense_kernel(Geom g, const __grid_constant__ LevelOp<doub
     const int p = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     int i, j, k;
     if (p >= g.npad || !slot_node(g, p, i, j, k)) return;
-    const bool interior = KIND == OP_DENSE ? true : is_interior(g, i, j, k);
+    const bool interior = (KIND == OP_DENSE || KIND == OP_PLANE) ? true : is_interior(g, i, j, k);
     double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (interior || b == 13) {
         LameRow<double> L;
@@ -255,7 +274,7 @@ __global__ void expand_dense_kernel(Geom g, const __grid_constant__ LevelOp<doub
             NbrOffsets nb = nbr_offsets(g, i, j, k);
             lame_faces(op.lop, g, nb, p, L, mu_nb, lam_nb);
         }
-        fine_block<KIND>(op, g, p, interior, mu_nb, lam_nb, L, b, a);
+        fine_block<KIND>(op, g, KIND == OP_PLANE ? k : p, interior, mu_nb, lam_nb, L, b, a);
     }
     const size_t np = (size_t)g.npad;
     for (int e = 0; e < 9; e++) coef[(size_t)(9 * b + e) * np + p] = a[e];
@@ -267,19 +286,36 @@ void launch_expand_dense(const LevelOp<double> &op, const Geom &g, double *coef,
     switch (op.kind) {
         case OP_CONST: expand_dense_kernel<OP_CONST><<<grid, kRB, 0, st>>>(g, op, coef); break;
         case OP_LAME: expand_dense_kernel<OP_LAME><<<grid, kRB, 0, st>>>(g, op, coef); break;
+        case OP_PLANE: expand_dense_kernel<OP_PLANE><<<grid, kRB, 0, st>>>(g, op, coef); break;
         default: expand_dense_kernel<OP_DENSE><<<grid, kRB, 0, st>>>(g, op, coef); break;
     }
 }
 
-void launch_rat(const LevelOp<double> &fine, const Geom &gf, const Geom &gc, double *coef_c, cudaStream_t st) {
+void launch_rat(const LevelOp<double> &fine, const Geom &gf, const Geom &gc, double *coef_c, bool plane,
+                cudaStream_t st) {
+    if (plane) {
+        cudaMemsetAsync(coef_c, 0, sizeof(double) * 243 * (size_t)gc.o, st);
+        dim3 grid((gc.o + kRB - 1) / kRB, 27);
+        if (fine.kind == OP_CONST) rat_kernel<OP_CONST, true><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c);
+        else rat_kernel<OP_PLANE, true><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c);
+        return;
+    }
     cudaMemsetAsync(coef_c, 0, sizeof(double) * 243 * (size_t)gc.npad, st);
     dim3 grid((gc.npad + kRB - 1) / kRB, 27);
     switch (fine.kind) {
-        case OP_CONST: rat_kernel<OP_CONST><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
-        case OP_LAME: rat_kernel<OP_LAME><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
-        default: rat_kernel<OP_DENSE><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
+        case OP_CONST: rat_kernel<OP_CONST, false><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
+        case OP_LAME: rat_kernel<OP_LAME, false><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
+        case OP_PLANE: rat_kernel<OP_PLANE, false><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
+        default: rat_kernel<OP_DENSE, false><<<grid, kRB, 0, st>>>(gf, gc, fine, coef_c); break;
     }
 }
+
+template <typename T>
+void launch_plane_dinv(int O, const T *coef, T *dinv, int *bad, cudaStream_t st) {
+    plane_dinv_kernel<T><<<(O + 127) / 128, 128, 0, st>>>(O, coef, dinv, bad);
+}
+template void launch_plane_dinv<float>(int, const float *, float *, int *, cudaStream_t);
+template void launch_plane_dinv<double>(int, const double *, double *, int *, cudaStream_t);
 
 template <typename T>
 void launch_dense_dinv(const Geom &g, const T *coef, T *dinv, int *bad, cudaStream_t st) {

@@ -13,98 +13,125 @@
 // sub-position (0,1,1) of a coarse cell, restrict_partial (mask 145) splits
 // between the two y parents according to the cell's x-collapse flag.
 #include "launch.h"
+#include "transfer.cuh"
 
 namespace stzmg {
 
 constexpr int kTB = 256;
 
-// Weight of fine index f (unwrapped, f in {2I-1, 2I, 2I+1}) as a child of
-// coarse index I along one dimension: 1, 0.5, or 0 when f is not a child.
-__host__ __device__ inline double child_w(int I, int f, int mf, int prd) {
-    if (!prd && (f < 0 || f >= mf)) return 0.0;
-    const bool collapse_dim = !prd && !(mf & 1);   // last fine node coincides with last coarse node
-    if (f == 2 * I) return 1.0;                     // (2I < mf guaranteed by the range test above)
-    if (f == 2 * I - 1) return (collapse_dim && f == mf - 1) ? 1.0 : 0.5;
-    /* f == 2I + 1 */
-    return (collapse_dim && f == mf - 1) ? 0.0 : 0.5;
-}
-
-__device__ inline int wrapi(int a, int len) {
-    if (a < 0) return a + len;
-    if (a >= len) return a - len;
-    return a;
+// Restriction, one thread per coarse node on a 3-D grid (blockDim 32 x 8,
+// grid z = coarse planes).  Nodes away from non-periodic edges take the
+// regular path: all 27 children with the fixed weights (1/8)(1/2,1,1/2)^3.
+__device__ inline bool regular_dim(int I, int mc, int mf, int prd) {
+    if (prd) return true;
+    return I >= 1 && 2 * I + 1 < mf && ((mf & 1) || I < mc - 2);
 }
 
 template <typename T>
 __global__ void restriction_kernel(Geom gf, Geom gc, const T *__restrict__ res, T *__restrict__ rc) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x, I, J, K;
-    if (p >= gc.npad) return;
-    double acc[3] = {0.0, 0.0, 0.0};
-    if (slot_node(gc, p, I, J, K)) {
-        const bool xs = !gf.xp && !(gf.m & 1) && I == gc.m - 2;
-        for (int dz = -1; dz <= 1; dz++) {
-            int fz = 2 * K + dz;
-            double wz = child_w(K, fz, gf.o, gf.zp);
-            if (wz == 0.0) continue;
-            int fzw = wrapi(fz, gf.o);
-            for (int dy = -1; dy <= 1; dy++) {
-                int fy = 2 * J + dy;
-                double wy = child_w(J, fy, gf.n, gf.yp);
-                if (!gf.yp && (fy < 0 || fy >= gf.n)) continue;
-                int fyw = wrapi(fy, gf.n);
-                for (int dx = -1; dx <= 1; dx++) {
-                    int fx = 2 * I + dx;
-                    double wx = child_w(I, fx, gf.m, gf.xp);
-                    if (wx == 0.0) continue;
-                    double wyy = wy;
-                    if (dx == 0 && (fy & 1) && (fz & 1)) wyy = xs ? (dy < 0 ? 1.0 : 0.0) : 0.5;
-                    if (wyy == 0.0) continue;
-                    int s = slot(gf, wrapi(fx, gf.m), fyw, fzw);
-                    double w = 0.125 * wx * wyy * wz;
-                    acc[0] += w * (double)res[s];
-                    acc[1] += w * (double)res[s + gf.npad];
-                    acc[2] += w * (double)res[s + 2 * gf.npad];
+    const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
+    if (I >= gc.m || J >= gc.n) return;
+    const int p = slot(gc, I, J, K);
+    T acc[3] = {T(0), T(0), T(0)};
+    if (regular_dim(I, gc.m, gf.m, gf.xp) && regular_dim(J, gc.n, gf.n, gf.yp) && regular_dim(K, gc.o, gf.o, gf.zp)) {
+        int fx[3], fy[3], fz[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            fx[d] = wrapi(2 * I + d - 1, gf.m);
+            fy[d] = wrapi(2 * J + d - 1, gf.n);
+            fz[d] = wrapi(2 * K + d - 1, gf.o);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    // 0.125 * wx * wy * wz with w = 1 at the centre child, 1/2 off it
+                    const T w = T(0.125) * (c == 1 ? T(1) : T(0.5)) * (b == 1 ? T(1) : T(0.5)) * (a == 1 ? T(1) : T(0.5));
+                    T v[3];
+                    load3(res, gf.npad, slot(gf, fx[c], fy[b], fz[a]), v);
+                    acc[0] += w * v[0];
+                    acc[1] += w * v[1];
+                    acc[2] += w * v[2];
                 }
+    } else {
+        restrict_node<T>(gf, gc, res, p, I, J, K, acc);
+    }
+    rc[p] = acc[0];
+    rc[p + gc.npad] = acc[1];
+    rc[p + 2 * gc.npad] = acc[2];
+}
+
+// Interpolation, one thread per coarse cell (ci,cj,ck): the cell's 8 corner
+// values are loaded once and added, with the weights of P, to the fine nodes
+// 2c + s, s in {0,1}^3, that exist.  Every fine node belongs to exactly one
+// cell (c = f >> 1).
+template <typename T>
+__global__ void interpolation_kernel(Geom gf, Geom gc, const T *__restrict__ xc, T *__restrict__ xf) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x, cj = blockIdx.y * blockDim.y + threadIdx.y, ck = blockIdx.z;
+    if (ci >= gc.m || cj >= gc.n) return;
+    const int c[3] = {ci, cj, ck}, mc[3] = {gc.m, gc.n, gc.o}, mf[3] = {gf.m, gf.n, gf.o},
+              prd[3] = {gf.xp, gf.yp, gf.zp};
+    int up[3];      // wrapped c+1 (or -1)
+    bool ex[3][2];  // child s exists
+    bool col[3];    // child s=1 coincides with coarse c+1 (collapse)
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        up[d] = c[d] + 1 < mc[d] ? c[d] + 1 : (prd[d] ? 0 : -1);
+        ex[d][0] = 2 * c[d] < mf[d];
+        ex[d][1] = 2 * c[d] + 1 < mf[d];
+        col[d] = !prd[d] && !(mf[d] & 1) && 2 * c[d] + 1 == mf[d] - 1;
+    }
+    T v[2][2][2][3];
+#pragma unroll
+    for (int az = 0; az < 2; az++)
+#pragma unroll
+        for (int ay = 0; ay < 2; ay++)
+#pragma unroll
+            for (int ax = 0; ax < 2; ax++) {
+                const int X = ax ? up[0] : ci, Y = ay ? up[1] : cj, Z = az ? up[2] : ck;
+                if (X < 0 || Y < 0 || Z < 0) {
+                    v[az][ay][ax][0] = v[az][ay][ax][1] = v[az][ay][ax][2] = T(0);
+                } else {
+                    load3(xc, gc.npad, slot(gc, X, Y, Z), v[az][ay][ax]);
+                }
+            }
+#pragma unroll
+    for (int sz = 0; sz < 2; sz++) {
+        if (!ex[2][sz]) continue;
+#pragma unroll
+        for (int sy = 0; sy < 2; sy++) {
+            if (!ex[1][sy]) continue;
+#pragma unroll
+            for (int sx = 0; sx < 2; sx++) {
+                if (!ex[0][sx]) continue;
+                // parents per dimension: s = 0 -> {c}; s = 1 -> {c, c+1} or {c+1} (collapse)
+                const int z0 = (sz && col[2]) ? 1 : 0, z1 = sz && !col[2] ? 1 : z0;
+                const int y0 = (sy && col[1]) ? 1 : 0, y1 = sy && !col[1] ? 1 : y0;
+                const int x0 = (sx && col[0]) ? 1 : 0, x1 = sx && !col[0] ? 1 : x0;
+                T s3[3] = {T(0), T(0), T(0)};
+                int cnt = 0;
+#pragma unroll
+                for (int az = 0; az < 2; az++)
+#pragma unroll
+                    for (int ay = 0; ay < 2; ay++)
+#pragma unroll
+                        for (int ax = 0; ax < 2; ax++) {
+                            if (az < z0 || az > z1 || ay < y0 || ay > y1 || ax < x0 || ax > x1) continue;
+                            s3[0] += v[az][ay][ax][0];
+                            s3[1] += v[az][ay][ax][1];
+                            s3[2] += v[az][ay][ax][2];
+                            cnt++;
+                        }
+                const T w = T(1) / T(cnt);
+                const int p = slot(gf, 2 * ci + sx, 2 * cj + sy, 2 * ck + sz);
+                xf[p] += w * s3[0];
+                xf[p + gf.npad] += w * s3[1];
+                xf[p + 2 * gf.npad] += w * s3[2];
             }
         }
     }
-    rc[p] = (T)acc[0];
-    rc[p + gc.npad] = (T)acc[1];
-    rc[p + 2 * gc.npad] = (T)acc[2];
-}
-
-// Parents of fine index f (wrapped coarse indices) and their common weight.
-__device__ inline int parents(int f, int mf, int mc, int prd, int *c, double *w) {
-    if ((f & 1) == 0) { c[0] = f >> 1; *w = 1.0; return 1; }
-    if (!prd && !(mf & 1) && f == mf - 1) { c[0] = (f >> 1) + 1; *w = 1.0; return 1; }
-    c[0] = f >> 1;
-    c[1] = wrapi((f >> 1) + 1, mc);
-    *w = 0.5;
-    return 2;
-}
-
-template <typename T>
-__global__ void interpolation_kernel(Geom gf, Geom gc, const T *__restrict__ xc, T *__restrict__ xf) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x, i, j, k;
-    if (p >= gf.npad || !slot_node(gf, p, i, j, k)) return;
-    int cx[2], cy[2], cz[2];
-    double wx, wy, wz;
-    int nx = parents(i, gf.m, gc.m, gf.xp, cx, &wx);
-    int ny = parents(j, gf.n, gc.n, gf.yp, cy, &wy);
-    int nz = parents(k, gf.o, gc.o, gf.zp, cz, &wz);
-    T s[3] = {T(0), T(0), T(0)};
-    for (int a = 0; a < nz; a++)
-        for (int b = 0; b < ny; b++)
-            for (int c = 0; c < nx; c++) {
-                int q = slot(gc, cx[c], cy[b], cz[a]);
-                s[0] += xc[q];
-                s[1] += xc[q + gc.npad];
-                s[2] += xc[q + 2 * gc.npad];
-            }
-    const T w = (T)(wx * wy * wz);
-    xf[p] += w * s[0];
-    xf[p + gf.npad] += w * s[1];
-    xf[p + 2 * gf.npad] += w * s[2];
 }
 
 template <typename T>
@@ -175,17 +202,98 @@ __global__ void scale_kernel(double *__restrict__ v, double s, size_t n) {
     for (; t < n; t += (size_t)gridDim.x * blockDim.x) v[t] *= s;
 }
 
+// x = Ainv r with one warp per row (Ainv row-major, lanes stride the columns).
 template <typename T>
-__global__ void bottom_direct_kernel(int nrow, const double *__restrict__ ainv_t, const int *__restrict__ nat_slot,
+__global__ void bottom_direct_kernel(int nrow, const double *__restrict__ ainv, const int *__restrict__ nat_slot,
                                      int npad, const T *__restrict__ r, T *__restrict__ x) {
-    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= nrow) return;
     double acc = 0.0;
-    for (int col = 0; col < nrow; col++) {
+    const double *a = ainv + (size_t)row * nrow;
+    for (int col = lane; col < nrow; col += 32) {
         int s = nat_slot[col / 3] + (col % 3) * npad;
-        acc += ainv_t[(size_t)col * nrow + row] * (double)r[s];
+        acc += a[col] * (double)r[s];
     }
-    x[nat_slot[row / 3] + (row % 3) * npad] = (T)acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[nat_slot[row / 3] + (row % 3) * npad] = (T)acc;
+}
+
+// ---------------------------------------------------------------- bottom inverse
+// Gauss-Jordan elimination with partial pivoting on the augmented matrix
+// [M | I] (n x 2n, row-major, FP64); afterwards the right half is M^-1.
+// Column c: pivot search (one block), row swap + scaling + copy of column c,
+// then elimination of column c from every other row.
+__global__ void gj_pivot_kernel(const double *__restrict__ a, int n, int c, int *piv, int *bad) {
+    __shared__ double bv[1024];
+    __shared__ int bi[1024];
+    double best = -1.0;
+    int arg = c;
+    for (int r = c + threadIdx.x; r < n; r += blockDim.x) {
+        double v = fabs(a[(size_t)r * 2 * n + c]);
+        if (v > best) { best = v; arg = r; }
+    }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = arg;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            double v2 = bv[threadIdx.x + o];
+            int i2 = bi[threadIdx.x + o];
+            if (v2 > bv[threadIdx.x] || (v2 == bv[threadIdx.x] && i2 < bi[threadIdx.x])) {
+                bv[threadIdx.x] = v2;
+                bi[threadIdx.x] = i2;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *piv = bi[0];
+        if (!(bv[0] > 0.0) || !(bv[0] - bv[0] == 0.0)) atomicExch(bad, 1);
+    }
+}
+
+__global__ void gj_swap_scale_kernel(double *__restrict__ a, int n, int c, const int *piv, double *__restrict__ col) {
+    const int p = *piv;
+    const size_t w = 2 * (size_t)n;
+    // swap rows c and p
+    for (int q = threadIdx.x; q < 2 * n; q += blockDim.x) {
+        double t = a[(size_t)c * w + q];
+        a[(size_t)c * w + q] = a[(size_t)p * w + q];
+        a[(size_t)p * w + q] = t;
+    }
+    __syncthreads();
+    const double inv = 1.0 / a[(size_t)c * w + c];
+    __syncthreads();
+    for (int q = threadIdx.x; q < 2 * n; q += blockDim.x) a[(size_t)c * w + q] *= inv;
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += blockDim.x) col[r] = r == c ? 0.0 : a[(size_t)r * w + c];
+}
+
+__global__ void gj_eliminate_kernel(double *__restrict__ a, int n, int c, const double *__restrict__ col) {
+    const size_t w = 2 * (size_t)n;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (q >= 2 * n) return;
+    const double f = col[r];
+    if (f != 0.0) a[(size_t)r * w + q] -= f * a[(size_t)c * w + q];
+}
+
+__global__ void gj_extract_kernel(const double *__restrict__ a, int n, double *__restrict__ inv) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * n) return;
+    size_t r = t / n, q = t % n;
+    inv[t] = a[r * 2 * n + n + q];
+}
+
+void launch_gauss_jordan(double *aug, int n, double *inv, int *piv, double *col, int *bad, cudaStream_t st) {
+    dim3 eg((2 * n + 255) / 256, n);
+    for (int c = 0; c < n; c++) {
+        gj_pivot_kernel<<<1, 1024, 0, st>>>(aug, n, c, piv, bad);
+        gj_swap_scale_kernel<<<1, 1024, 0, st>>>(aug, n, c, piv, col);
+        gj_eliminate_kernel<<<eg, 256, 0, st>>>(aug, n, c, col);
+    }
+    gj_extract_kernel<<<(unsigned)(((size_t)n * n + 255) / 256), 256, 0, st>>>(aug, n, inv);
 }
 
 static inline unsigned blocks_for(long n) { return (unsigned)((n + kTB - 1) / kTB); }
@@ -196,11 +304,13 @@ static inline unsigned grid_stride_blocks(size_t n) {
 
 template <typename T>
 void launch_restriction(const Geom &gf, const Geom &gc, const T *res_f, T *r_c, cudaStream_t st) {
-    restriction_kernel<T><<<blocks_for(gc.npad), kTB, 0, st>>>(gf, gc, res_f, r_c);
+    dim3 blk(32, 8), grd((gc.m + 31) / 32, (gc.n + 7) / 8, gc.o);
+    restriction_kernel<T><<<grd, blk, 0, st>>>(gf, gc, res_f, r_c);
 }
 template <typename T>
 void launch_interpolation(const Geom &gf, const Geom &gc, const T *x_c, T *x_f, cudaStream_t st) {
-    interpolation_kernel<T><<<blocks_for(gf.npad), kTB, 0, st>>>(gf, gc, x_c, x_f);
+    dim3 blk(32, 8), grd((gc.m + 31) / 32, (gc.n + 7) / 8, gc.o);
+    interpolation_kernel<T><<<grd, blk, 0, st>>>(gf, gc, x_c, x_f);
 }
 template <typename T>
 void launch_nat_to_cb(const Geom &g, const double *nat, T *cb, cudaStream_t st) {
@@ -232,7 +342,7 @@ void launch_scale(double *v, double s, size_t n, cudaStream_t st) {
 template <typename T>
 void launch_bottom_direct(int nrow, const double *ainv_t, const int *nat_slot, int npad, const T *r, T *x,
                           cudaStream_t st) {
-    bottom_direct_kernel<T><<<blocks_for(nrow), kTB, 0, st>>>(nrow, ainv_t, nat_slot, npad, r, x);
+    bottom_direct_kernel<T><<<blocks_for(32L * nrow), kTB, 0, st>>>(nrow, ainv_t, nat_slot, npad, r, x);
 }
 
 template void launch_restriction<float>(const Geom &, const Geom &, const float *, float *, cudaStream_t);

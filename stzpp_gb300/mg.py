@@ -34,12 +34,16 @@ FIELD_X, FIELD_R = 0, 1
 EXPORTS = (
     "stz_mg_desc_default", "stz_mg_last_error", "stz_mg_create", "stz_mg_destroy",
     "stz_mg_set_stencil_const", "stz_mg_set_stencil_points", "stz_mg_set_coeffs_lame", "stz_mg_setup",
-    "stz_mg_set_rhs", "stz_mg_set_x", "stz_mg_get_x", "stz_mg_vcycle", "stz_mg_solve",
-    "stz_mg_residual_norm", "stz_mg_l2_error_all", "stz_mg_num_levels", "stz_mg_level_dims",
+    "stz_mg_set_rhs", "stz_mg_set_x", "stz_mg_get_x", "stz_mg_get_rhs", "stz_mg_set_rhs_divergence",
+    "stz_mg_vcycle", "stz_mg_solve",
+    "stz_mg_solve_stats", "stz_mg_residual_norm", "stz_mg_l2_error_all", "stz_mg_num_levels", "stz_mg_level_dims",
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
-    "stz_mg_level_residual",
+    "stz_mg_level_residual", "stz_mg_time_kernel",
 )
+
+# measurement hook kernel ids (include/stz_mg.h)
+K_GS_COLOUR, K_RESIDUAL, K_RESTRICT, K_INTERP, K_RESIDUAL64 = range(5)
 
 
 class StzMgError(RuntimeError):
@@ -53,7 +57,7 @@ class Desc(ctypes.Structure):
                 ("x_prd", ctypes.c_int), ("y_prd", ctypes.c_int), ("z_prd", ctypes.c_int),
                 ("precision", ctypes.c_int), ("v_down", ctypes.c_int), ("v_up", ctypes.c_int),
                 ("max_coarse", ctypes.c_int), ("bottom", ctypes.c_int), ("bottom_sweeps", ctypes.c_int),
-                ("device", ctypes.c_int), ("stream", ctypes.c_void_p)]
+                ("sweep_growth", ctypes.c_int), ("device", ctypes.c_int), ("stream", ctypes.c_void_p)]
 
 
 _lib = None
@@ -77,10 +81,12 @@ def load_library():
     lib.stz_mg_set_stencil_points.argtypes = [vp, vp, ci]
     lib.stz_mg_set_coeffs_lame.argtypes = [vp, vp, vp, cd, cd, cd, cd, ci]
     lib.stz_mg_setup.argtypes = [vp]
-    for f in ("stz_mg_set_rhs", "stz_mg_set_x", "stz_mg_get_x"):
+    lib.stz_mg_set_rhs_divergence.argtypes = [vp, vp, cd, cd, cd, ci]
+    for f in ("stz_mg_set_rhs", "stz_mg_set_x", "stz_mg_get_x", "stz_mg_get_rhs"):
         getattr(lib, f).argtypes = [vp, vp, ci]
     lib.stz_mg_vcycle.argtypes = [vp]
     lib.stz_mg_solve.argtypes = [vp, cd, ci, ctypes.POINTER(ci), ctypes.POINTER(cd)]
+    lib.stz_mg_solve_stats.argtypes = [vp, ctypes.POINTER(ci), ctypes.POINTER(ci), ctypes.POINTER(ctypes.c_longlong)]
     lib.stz_mg_residual_norm.argtypes = [vp, ctypes.POINTER(cd), ctypes.POINTER(cd)]
     lib.stz_mg_l2_error_all.argtypes = [vp, ctypes.POINTER(cd)]
     lib.stz_mg_num_levels.argtypes = [vp, ctypes.POINTER(ci)]
@@ -92,6 +98,7 @@ def load_library():
     lib.stz_mg_level_restriction.argtypes = [vp, ci]
     lib.stz_mg_level_interpolation.argtypes = [vp, ci]
     lib.stz_mg_level_residual.argtypes = [vp, ci, vp, ctypes.POINTER(cd), ci]
+    lib.stz_mg_time_kernel.argtypes = [vp, ci, ci, ci, ctypes.POINTER(cd), ctypes.POINTER(cd)]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci
@@ -165,10 +172,11 @@ class Multigrid:
     ``max_coarse`` (reference: 1024).  ``precision`` is "fp64" or "mixed"
     (FP32 V-cycles inside FP64 defect correction); ``bottom`` is "direct"
     (FP64 dense solve of the coarsest level) or "gs" (``bottom_sweeps``
-    Gauss-Seidel sweeps, the reference's solve_exact)."""
+    Gauss-Seidel sweeps, the reference's solve_exact).  ``sweep_growth`` keeps
+    the reference's 2+i sweeps on level i; False uses v_down/v_up everywhere."""
 
     def __init__(self, dims, periodic=(True, True, False), precision="fp64", v_down=2, v_up=2,
-                 max_coarse=16, bottom="direct", bottom_sweeps=24, device=0, stream=None):
+                 max_coarse=1024, bottom="direct", bottom_sweeps=24, sweep_growth=True, device=0, stream=None):
         lib = load_library()
         d = Desc()
         lib.stz_mg_desc_default(ctypes.byref(d))
@@ -179,6 +187,7 @@ class Multigrid:
         d.max_coarse = max_coarse
         d.bottom = {"direct": BOTTOM_DIRECT, "gs": BOTTOM_GS}[bottom]
         d.bottom_sweeps = bottom_sweeps
+        d.sweep_growth = int(bool(sweep_growth))
         d.device = device
         d.stream = stream
         self.dims = tuple(int(v) for v in dims)
@@ -253,6 +262,22 @@ class Multigrid:
         if r is not None:
             self.set_rhs(r)
 
+    def set_rhs_divergence(self, eps, spacing):
+        """Right-hand side = node divergence of the cell tensor field eps
+        (6 components per cell), assembled on the device."""
+        m, n, o = self.dims
+        xp, yp, zp = self.periodic
+        ncells = (m if xp else m - 1) * (n if yp else n - 1) * (o if zp else o - 1)
+        p, where, keep = _arg(eps, 6 * ncells)
+        _check(load_library().stz_mg_set_rhs_divergence(self._h, p, *spacing, where))
+
+    def get_rhs(self, out=None):
+        if out is None:
+            out = np.empty((self.npts, 3))
+        p, where, keep = _arg(out, 3 * self.npts)
+        _check(load_library().stz_mg_get_rhs(self._h, p, where))
+        return out
+
     def get_x(self, out=None):
         if out is None:
             out = np.empty((self.npts, 3))
@@ -271,6 +296,12 @@ class Multigrid:
         if rc != OK and (check or rc != ERR_NOCONV):
             _check(rc)
         return c.value, r.value
+
+    def solve_stats(self):
+        """(V-cycles, FP64 residual evaluations, kernels launched) of the last solve."""
+        c, r, k = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _check(load_library().stz_mg_solve_stats(self._h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(k)))
+        return c.value, r.value, k.value
 
     def residual_norm(self):
         rn, bn = ctypes.c_double(), ctypes.c_double()
@@ -332,3 +363,10 @@ class Multigrid:
         _check(load_library().stz_mg_level_residual(self._h, l, out.ctypes.data_as(ctypes.c_void_p),
                                                     ctypes.byref(sq), HOST))
         return out, sq.value
+
+    def time_kernel(self, kernel, level=0, reps=20):
+        """(ms per launch, algorithmic bytes or FP64 flops per launch) of one
+        solver kernel, timed with CUDA events on the handle's stream."""
+        ms, work = ctypes.c_double(), ctypes.c_double()
+        _check(load_library().stz_mg_time_kernel(self._h, kernel, level, reps, ctypes.byref(ms), ctypes.byref(work)))
+        return ms.value, work.value

@@ -44,7 +44,8 @@ def test_desc_defaults(lib):
     from stzpp_gb300.mg import Desc
     d = Desc()
     lib.stz_mg_desc_default(ctypes.byref(d))
-    assert (d.precision, d.v_down, d.v_up, d.max_coarse, d.bottom, d.bottom_sweeps) == (0, 2, 2, 16, 0, 24)
+    assert (d.precision, d.v_down, d.v_up, d.max_coarse, d.bottom, d.bottom_sweeps, d.sweep_growth) == \
+        (0, 2, 2, 1024, 0, 24, 1)
 
 
 def test_create_rejects_bad_arguments(lib):
