@@ -1,0 +1,107 @@
+"""Generates the golden fixtures of the multigrid from the compiled reference.
+
+Needs oracle/_ref/libstzref.so, i.e. the reference's own mg_3d_template
+sources compiled by ``make -C oracle ref`` where the reference checkout is
+available.  Writes tests/golden/reference_small.npz, which the CPU tests use
+to pin the C restatement of the reference (oracle/stzmg_oracle.c) on machines
+without the reference.
+
+Cases (all seeded):
+  * ``p110``: 8x8x9, periodic x,y, Dirichlet z, constant elasticity stencil
+    (mu=1, lambda=2, dx=1/8), hierarchy extended to 2x2x3 (max_coarse 16);
+  * ``d000``: 6x5x4, all Dirichlet (even sizes: the collapse masks and the
+    restrict_partial mask-145 quirk), hierarchy to <= 8 nodes;
+  * ``var``: 8x8x9 periodic x,y with lognormal mu (seed 1), lambda = 2 mu,
+    per-node stencils through fill_entries;
+  * ``cfg1``: the 32x32x33 problem (dx=1/32), reference hierarchy and cycle
+    (lexicographic GS, 24 bottom sweeps): residual history of the solve to
+    1e-10 and a strided subsample of the solution.
+For each small case: box bounds S and coefficients of every level, one GS
+sweep, restriction, interpolation and two V-cycles from seeded fields.
+
+Run: python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import problem as P  # noqa: E402
+from oracle import refpy  # noqa: E402
+
+
+def build(dims, per, kind, max_coarse):
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per)
+    if kind == "const":
+        st, fix = P.elastic_stencil_const(1.0, 2.0, *h)
+        return refpy.RefMultigrid(dims, per, stencil=st, fix=fix, max_coarse=max_coarse)
+    mu = P.lognormal_mu(1, m, n, o)
+    return refpy.RefMultigrid(dims, per, points=P.elastic_stencil_points(mu, 2 * mu, *h, per), max_coarse=max_coarse)
+
+
+def small_case(out, name, dims, per, kind, max_coarse):
+    R = build(dims, per, kind, max_coarse)
+    L = R.nlevels
+    out[f"{name}/nlevels"] = np.int32(L)
+    for l in range(L):
+        out[f"{name}/dims{l}"] = np.array(R.level_dims(l), dtype=np.int32)
+        out[f"{name}/S{l}"] = R.level_S(l).astype(np.int8)
+        if l > 0:
+            out[f"{name}/A{l}"] = R.level_A(l)
+    rng = np.random.default_rng(11)
+    N0 = R.npts(0)
+    x0, b0 = rng.standard_normal((N0, 3)), rng.standard_normal((N0, 3))
+    out[f"{name}/x0"], out[f"{name}/b0"] = x0, b0
+    R.set_field(0, "x", x0)
+    R.set_field(0, "r", b0)
+    R.gauss_seidel(0, 1)
+    out[f"{name}/gs0"] = R.get_field(0, "x")
+    R.restriction(1)
+    out[f"{name}/restrict1"] = R.get_field(1, "r")
+    xc = rng.standard_normal((R.npts(1), 3))
+    out[f"{name}/xc1"] = xc
+    R.set_field(1, "x", xc)
+    R.interpolation(1)
+    out[f"{name}/interp0"] = R.get_field(0, "x")
+    R.set_field(0, "x", x0)
+    R.set_field(0, "r", b0)
+    R.v_cycle("gs")
+    R.v_cycle("gs")
+    out[f"{name}/vcycle2"] = R.get_field(0, "x")
+    R.close()
+
+
+def main():
+    if not refpy.available():
+        sys.exit("oracle/_ref/libstzref.so is missing: run `make -C oracle ref` where the reference is available")
+    out = {}
+    small_case(out, "p110", (8, 8, 9), (True, True, False), "const", 16)
+    small_case(out, "d000", (6, 5, 4), (False, False, False), "const", 8)
+    small_case(out, "var", (8, 8, 9), (True, True, False), "var", 16)
+    # the 32x32x33 problem with the reference's own solver
+    m, n, o = 32, 32, 33
+    per = (True, True, False)
+    h = P.grid_spacing(m, n, o, per)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    R = build((m, n, o), per, "const", 1024)
+    R.set_field(0, "r", b)
+    R.set_field(0, "x", np.zeros_like(b))
+    cycles, hist = R.solve(1e-10, 100)
+    x = R.get_field(0, "x")
+    out["cfg1/hist"] = hist
+    out["cfg1/x_sub"] = x[::97]
+    out["cfg1/x_norm"] = np.float64(np.linalg.norm(x))
+    out["cfg1/b_norm"] = np.float64(np.linalg.norm(b))
+    R.close()
+    path = os.path.join(HERE, "reference_small.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes;", "cfg1 cycles", cycles)
+
+
+if __name__ == "__main__":
+    main()
