@@ -162,6 +162,40 @@ enum {
 int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
                        double *work_per_launch);
 
+/* Allocation-free residual check (no counterpart in the reference).
+ *
+ * Computes sum over nodes of |b - A x|^2, where A is one shared 27-block
+ * stencil on interior nodes and one fix block on Dirichlet nodes (the
+ * external_ptr form of shear_sim_3d.hh:401-402; same stencil and fix layout as
+ * stz_mg_set_stencil_const), for fields x and b that the caller already holds
+ * on `device` in the natural layout (3 doubles per node, node
+ * i + m*(j + n*k)).  The result is stored, not accumulated, into the device
+ * double *sumsq; the kernels are queued on `stream` (a cudaStream_t of that
+ * device, NULL for the legacy default stream) and the call returns without
+ * waiting for them.  No handle is needed.
+ *
+ * It is meant for callers that must not allocate at the point of the check:
+ * cudaMalloc and cudaFree can synchronise the whole device, stalling the
+ * caller's work in flight on other streams, and an allocation can fail when
+ * the caller's own fields already fill the GPU's memory.  The call allocates
+ * nothing (no cudaMalloc, no cudaFree, no pinned host memory): its partial
+ * sums live in a fixed device array of STZ_MG_NOALLOC_PARTIALS doubles
+ * (1 MiB) compiled into the library, which limits it to grids of at most
+ * STZ_MG_NOALLOC_MAX_NODES nodes; larger grids get STZ_MG_ERR_ARG and
+ * stz_mg_residual_norm does the job.  No memory has to start at zero.
+ *
+ * All calls on one device share that array: calls whose kernels may run at
+ * the same time on one device (different streams, or host threads without
+ * ordering) race and corrupt each other's results, so keep them on one stream
+ * or order them with events.  The first call on a device looks up the array's
+ * device address (once per device); make that first call before any stream
+ * capture begins. */
+#define STZ_MG_NOALLOC_PARTIALS 131072
+#define STZ_MG_NOALLOC_MAX_NODES (1024LL * STZ_MG_NOALLOC_PARTIALS)
+int stz_mg_const_residual_sumsq_noalloc(int m, int n, int o, int x_prd, int y_prd, int z_prd,
+                                        const double *stencil, const double *fix, const double *x,
+                                        const double *b, double *sumsq, int device, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

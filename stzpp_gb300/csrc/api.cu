@@ -1241,3 +1241,12 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
 }
 
 }  // extern "C"
+
+namespace stzmg {
+// Sets the text stz_mg_last_error() returns, for entry points defined in other
+// translation units.
+int record_error(int code, const char *msg) {
+    g_last_error = msg;
+    return code;
+}
+}  // namespace stzmg

@@ -39,7 +39,7 @@ EXPORTS = (
     "stz_mg_solve_stats", "stz_mg_residual_norm", "stz_mg_l2_error_all", "stz_mg_num_levels", "stz_mg_level_dims",
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
-    "stz_mg_level_residual", "stz_mg_time_kernel",
+    "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
@@ -99,6 +99,7 @@ def load_library():
     lib.stz_mg_level_interpolation.argtypes = [vp, ci]
     lib.stz_mg_level_residual.argtypes = [vp, ci, vp, ctypes.POINTER(cd), ci]
     lib.stz_mg_time_kernel.argtypes = [vp, ci, ci, ci, ctypes.POINTER(cd), ctypes.POINTER(cd)]
+    lib.stz_mg_const_residual_sumsq_noalloc.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, ci, vp]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci
