@@ -129,6 +129,30 @@ int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm);
  * reference sums |r|^4 (its mg3d_mod_sq squares the vec3 -> double cast). */
 int stz_mg_l2_error_all(stz_mg_handle h, double *out);
 
+/* Adjoint of the projection solve (no counterpart in the reference, whose
+ * solver is not differentiated).  For a scalar loss L(u) with u = A^{-1} b:
+ *   dL/db = w with A^T w = g, g = dL/du,
+ *   dL/dmu_p, dL/dlam_p = -w^T (dA/dmu_p) u, -w^T (dA/dlam_p) u.
+ *
+ * stz_mg_adjoint_solve solves A^T w = g (npts*3 doubles in natural order,
+ * from/to host or device memory per `where`) for a top-level operator set by
+ * stz_mg_set_stencil_const (symmetric blocks, S[d] = S[-d]^T, as the
+ * elasticity stencil of shear_sim_3d.cpp:215-331) or stz_mg_set_coeffs_lame.
+ * The interior block of such an A is symmetric, so the interior part of w is
+ * the handle's own V-cycle solve of A y = g with g zeroed on the Dirichlet
+ * nodes (rel_tol, max_cycles, cycles, relres as in stz_mg_solve, relative to
+ * that masked g); the Dirichlet part follows from F^T w_D = g_D - A_ID^T w_I.
+ * It overwrites the handle's x and right-hand side (save u first).
+ *
+ * stz_mg_coeff_grad contracts w and u (npts*3 each) into dmu, dlam (npts
+ * each) for the Lame operator of stz_mg_set_coeffs_lame, with the same
+ * discretisation the solver applies (face-midpoint averages, node values on
+ * the edge terms, the fix blocks of the Dirichlet nodes).  It does not solve
+ * anything and leaves x and the right-hand side alone. */
+int stz_mg_adjoint_solve(stz_mg_handle h, const double *g, double *w, int where, double rel_tol, int max_cycles,
+                         int *cycles, double *relres);
+int stz_mg_coeff_grad(stz_mg_handle h, const double *w, const double *u, double *dmu, double *dlam, int where);
+
 /* Level-wise operations on the FP64 hierarchy, the region members the
  * reference's multigrid class calls (used for parity checks). */
 int stz_mg_num_levels(stz_mg_handle h, int *nlevels);

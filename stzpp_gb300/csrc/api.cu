@@ -105,6 +105,8 @@ struct stz_mg_handle_s {
     int *dflag = nullptr;
     double *stage = nullptr;    // device staging for host<->device natural-order copies
     size_t stage_len = 0;
+    double *adj_g = nullptr, *adj_t = nullptr;   // adjoint: natural-order g and work vector
+    double *grad_c = nullptr;                    // coefficient gradient: 14 doubles per node
     double bnorm = -1.0;
     bool setup_done = false;
     cudaGraphExec_t gx64 = nullptr, gx32 = nullptr;
@@ -999,6 +1001,86 @@ int stz_mg_residual_norm(stz_mg_handle h, double *rnorm, double *bnorm) {
         double rs = top_residual_sq(h, nullptr);
         if (rnorm) *rnorm = std::sqrt(rs);
         if (bnorm) *bnorm = rhs_norm(h);
+    });
+}
+
+int stz_mg_adjoint_solve(stz_mg_handle h, const double *g, double *w, int where, double rel_tol, int max_cycles,
+                         int *cycles, double *relres) {
+    if (!h || !g || !w) return set_error(STZ_MG_ERR_ARG, "null argument");
+    if (!(rel_tol > 0) || max_cycles < 0) return set_error(STZ_MG_ERR_ARG, "bad tolerance or cycle cap");
+    if (where != STZ_MG_HOST && where != STZ_MG_DEVICE)
+        return set_error(STZ_MG_ERR_ARG, "where must be STZ_MG_HOST or STZ_MG_DEVICE");
+    return guarded(h, [&] {
+        need_setup(h);
+        const LevelOp<double> &top = h->op64[0];
+        if (top.kind != OP_CONST && top.kind != OP_LAME)
+            fail(STZ_MG_ERR_UNSUPPORTED, "the adjoint solve needs a shared-stencil or Lame top-level operator");
+        if (top.kind == OP_CONST) {
+            // A_II^T = A_II needs S[d] = S[-d]^T
+            for (int b = 0; b < 27; b++)
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        if (top.cop.a[b][3 * r + c] != top.cop.a[26 - b][3 * c + r])
+                            fail(STZ_MG_ERR_UNSUPPORTED, "the shared stencil is not symmetric (block %d)", b);
+        }
+        const Geom &g0 = h->geo[0];
+        const size_t n3 = 3 * npts(g0);
+        if (!h->adj_g) {
+            h->adj_g = h->alloc<double>(n3);
+            h->adj_t = h->alloc<double>(n3);
+        }
+        CK(cudaMemcpyAsync(h->adj_g, g, n3 * sizeof(double),
+                           where == STZ_MG_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->st));
+        require_finite(h, h->adj_g, n3, "adjoint right-hand side");
+        // interior part: A y = g' with g'_D = 0 gives y_D = 0 and A_II y_I = g_I
+        launch_mask_dirichlet(g0, h->adj_g, h->adj_t, h->st);
+        launch_nat_to_cb<double>(g0, h->adj_t, h->L64[0].r, h->st);
+        check_launch();
+        CK(cudaMemsetAsync(h->L64[0].x, 0, 3 * (size_t)g0.npad * sizeof(double), h->st));
+        h->bnorm = -1.0;
+        solve(h, rel_tol, max_cycles, cycles, relres);
+        // Dirichlet part, node by node
+        double *wd = where == STZ_MG_DEVICE ? w : h->adj_t;
+        launch_cb_to_nat<double>(g0, h->L64[0].x, wd, h->st);
+        launch_adjoint_dirichlet(top, g0, h->adj_g, wd, h->st);
+        check_launch();
+        if (where == STZ_MG_HOST) CK(cudaMemcpyAsync(w, wd, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_coeff_grad(stz_mg_handle h, const double *w, const double *u, double *dmu, double *dlam, int where) {
+    if (!h || !w || !u || !dmu || !dlam) return set_error(STZ_MG_ERR_ARG, "null argument");
+    if (where != STZ_MG_HOST && where != STZ_MG_DEVICE)
+        return set_error(STZ_MG_ERR_ARG, "where must be STZ_MG_HOST or STZ_MG_DEVICE");
+    return guarded(h, [&] {
+        if (h->top_kind != OP_LAME)
+            fail(STZ_MG_ERR_UNSUPPORTED, "coefficient gradients need the Lame operator (stz_mg_set_coeffs_lame)");
+        const Geom &g0 = h->geo[0];
+        const size_t n = npts(g0);
+        if (!h->grad_c) h->grad_c = h->alloc<double>(14 * n);
+        if (!h->adj_g) {
+            h->adj_g = h->alloc<double>(3 * n);
+            h->adj_t = h->alloc<double>(3 * n);
+        }
+        const double *wd = w, *ud = u;
+        double *om = dmu, *ol = dlam;
+        if (where == STZ_MG_HOST) {
+            CK(cudaMemcpyAsync(h->adj_g, w, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+            CK(cudaMemcpyAsync(h->adj_t, u, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+            wd = h->adj_g;
+            ud = h->adj_t;
+            double *st = staging(h, 2 * n);
+            om = st;
+            ol = st + n;
+        }
+        launch_lame_grad(h->op64[0].lop, g0, wd, ud, h->grad_c, om, ol, h->st);
+        check_launch();
+        if (where == STZ_MG_HOST) {
+            CK(cudaMemcpyAsync(dmu, om, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaMemcpyAsync(dlam, ol, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        }
+        sync(h);
     });
 }
 

@@ -66,6 +66,18 @@ void launch_gauss_jordan(double *aug, int n, double *inv, int *piv, double *col,
 void launch_rhs_divergence(const Geom &g, const double *eps, double dx, double dy, double dz, double *r,
                            cudaStream_t st);
 
+// adjoint.cu (natural-order vec3 fields, 3 doubles per node)
+// dst = src with the rows of Dirichlet nodes zeroed
+void launch_mask_dirichlet(const Geom &g, const double *src, double *dst, cudaStream_t st);
+// w_D = F^{-T} (g_D - A_ID^T w_I) on the Dirichlet nodes of the top level
+// (OP_CONST or OP_LAME), given w on the interior nodes
+void launch_adjoint_dirichlet(const LevelOp<double> &top, const Geom &g, const double *gv, double *w,
+                              cudaStream_t st);
+// dmu, dlam = -w^T (dA/dmu, dA/dlam) u per node of the Lame operator; C is
+// scratch of 14 doubles per node
+void launch_lame_grad(const LameOp<double> &op, const Geom &g, const double *w, const double *u, double *C,
+                      double *dmu, double *dlam, cudaStream_t st);
+
 // tail.cu: persistent cluster kernels for the small levels lo..hi (hi+1 is
 // the bottom level).  Levels must be OP_PLANE or OP_DENSE.
 constexpr int kTailThreads = 1024;

@@ -40,6 +40,7 @@ EXPORTS = (
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
     "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
+    "stz_mg_adjoint_solve", "stz_mg_coeff_grad",
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
@@ -100,6 +101,8 @@ def load_library():
     lib.stz_mg_level_residual.argtypes = [vp, ci, vp, ctypes.POINTER(cd), ci]
     lib.stz_mg_time_kernel.argtypes = [vp, ci, ci, ci, ctypes.POINTER(cd), ctypes.POINTER(cd)]
     lib.stz_mg_const_residual_sumsq_noalloc.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, ci, vp]
+    lib.stz_mg_adjoint_solve.argtypes = [vp, vp, vp, ci, cd, ci, ctypes.POINTER(ci), ctypes.POINTER(cd)]
+    lib.stz_mg_coeff_grad.argtypes = [vp, vp, vp, vp, vp, ci]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci
@@ -314,6 +317,45 @@ class Multigrid:
         v = ctypes.c_double()
         _check(load_library().stz_mg_l2_error_all(self._h, ctypes.byref(v)))
         return v.value
+
+    # ------------------------------------------------------------- adjoint
+    def adjoint_solve(self, g, out=None, tol=1e-10, max_cycles=100):
+        """w with A^T w = g (overwrites the handle's x and right-hand side).
+        Returns (w, cycles, relres)."""
+        pg, wg, keep = _arg(g, 3 * self.npts)
+        if out is None:
+            if wg == DEVICE:
+                import torch
+                out = torch.empty_like(g)
+            else:
+                out = np.empty((self.npts, 3))
+        po, wo, keep2 = _arg(out, 3 * self.npts)
+        if wo != wg:
+            raise ValueError("g and out must both be host or both be device arrays")
+        c, r = ctypes.c_int(), ctypes.c_double()
+        _check(load_library().stz_mg_adjoint_solve(self._h, pg, po, wg, tol, max_cycles, ctypes.byref(c),
+                                                   ctypes.byref(r)))
+        return out, c.value, r.value
+
+    def coeff_grad(self, w, u, dmu=None, dlam=None):
+        """(-w^T dA/dmu u, -w^T dA/dlam u) per node of the Lame operator."""
+        pw, ww, k1 = _arg(w, 3 * self.npts)
+        pu, wu, k2 = _arg(u, 3 * self.npts)
+        if ww != wu:
+            raise ValueError("w and u must both be host or both be device arrays")
+        if dmu is None:
+            if ww == DEVICE:
+                import torch
+                dmu = torch.empty(self.npts, dtype=torch.float64, device=w.device)
+                dlam = torch.empty(self.npts, dtype=torch.float64, device=w.device)
+            else:
+                dmu, dlam = np.empty(self.npts), np.empty(self.npts)
+        pm, wm, k3 = _arg(dmu, self.npts)
+        pl, wl, k4 = _arg(dlam, self.npts)
+        if not (wm == wl == ww):
+            raise ValueError("all arrays must be on the same side")
+        _check(load_library().stz_mg_coeff_grad(self._h, pw, pu, pm, pl, ww))
+        return dmu, dlam
 
     # -------------------------------------------------------------- levels
     @property
