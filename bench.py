@@ -343,15 +343,158 @@ def run_ours(args, world, rank, local):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ config 3
+C3_DIMS = (512, 512, 257)
+C3_H = 1.0 / 256   # the grid spacing of the 257^3 problem on a 2 x 2 x 1 box
+
+
+def run_config3(args, local):
+    """512x512x257, lognormal mu (median 1, sigma 0.3, seed 1), lambda = 2 mu:
+    mixed vs FP64 GPU solve to 1e-10 and the mixed solution's error against
+    the FP64 one."""
+    import torch
+    torch.cuda.set_device(local)
+    import stzpp_gb300 as sg
+    from stzpp_gb300 import problems
+    dims, per, h = C3_DIMS, PERIODIC, (C3_H, C3_H, C3_H)
+    npts = dims[0] * dims[1] * dims[2]
+    stream = torch.cuda.current_stream()
+    mu_d = torch.from_numpy(problems.lognormal_mu(1, dims).reshape(-1)).cuda()
+    lam_d = 2 * mu_d
+    eps = torch.from_numpy(problems.random_strain(0, dims, per)).cuda()
+    res = {}
+    x_mixed = None
+    for prec in ("mixed", "fp64"):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        t0 = time.perf_counter()
+        mg = sg.Multigrid(dims, per, precision=prec, sweep_growth=False, device=local, stream=stream.cuda_stream)
+        mg.setup_matrices(mu=mu_d, lam=lam_d, spacing=h)
+        torch.cuda.synchronize()
+        setup_ms = (time.perf_counter() - t0) * 1e3
+        mem = free0 - torch.cuda.mem_get_info()[0]
+        mg.set_rhs_divergence(eps, h)
+        zero = torch.zeros(3 * npts, dtype=torch.float64, device="cuda")
+        steps = max(1, args.steps // (2 if prec == "mixed" else 3))
+        for _ in range(max(1, min(args.warmup, 2 if prec == "mixed" else 1))):
+            mg.set_x(zero)
+            mg.solve(TOL, 300)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            mg.set_x(zero)
+            cyc, rel = mg.solve(TOL, 300)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        x = torch.empty(3 * npts, dtype=torch.float64, device="cuda")
+        mg.get_x(x)
+        res[prec] = {"ms_per_solve": e0.elapsed_time(e1) / steps, "cycles": cyc, "relres": rel,
+                     "setup_ms": setup_ms, "device_bytes": int(mem), "levels": mg.nlevels}
+        mg.close()
+        if prec == "mixed":
+            x_mixed = x
+        else:
+            res["solution_rel_err_mixed_vs_fp64"] = float(torch.linalg.norm(x_mixed - x) / torch.linalg.norm(x))
+        del x
+    line = {"metric": "ms/solve to rel. residual 1e-10, mixed vs FP64 on GPU (512x512x257, lognormal mu)",
+            "value": res["mixed"]["ms_per_solve"], "unit": "ms", "higher_is_better": False,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "512x512x257 nodes, periodic x,y, Dirichlet z, h = 1/256, Lame operator with "
+                                   "lognormal mu (median 1, sigma 0.3, seed 1), lambda = 2 mu, RHS = divergence of "
+                                   "N(0,1e-3) cell strain (seed 0), x0 = 0, rel. residual 1e-10",
+                       "cycle": "V(2,2), 8-colour block GS, RAT (dense coarse levels), FP64 direct bottom"},
+            "mixed": res["mixed"], "fp64": res["fp64"],
+            "speedup_vs_fp64": res["fp64"]["ms_per_solve"] / res["mixed"]["ms_per_solve"],
+            "solution_rel_err_mixed_vs_fp64": res["solution_rel_err_mixed_vs_fp64"]}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ config 5
+def run_config5(args, local, T=50, every=10):
+    """50 warm-started mixed solves at 256x256x257 with a fixed lognormal mu,
+    b_t = b_{t-1} + divergence of an N(0,1e-5) strain-rate field (seeds from
+    3), loss sum_t |u_t - u*|^2 (u* ~ N(0,1e-3), seed 2); backward through all
+    solves with checkpointing every 10; gradient error against the FP64
+    solver (tolerance 1e-12) on the same sequence."""
+    import torch
+    torch.cuda.set_device(local)
+    from stzpp_gb300 import problems
+    from stzpp_gb300.autograd import ProjectionSolver, sequence_loss
+    dims, per = DIMS, PERIODIC
+    npts = dims[0] * dims[1] * dims[2]
+    h = problems.grid_spacing(dims, per)
+    ncells = dims[0] * dims[1] * (dims[2] - 1)
+    mu0 = torch.from_numpy(problems.lognormal_mu(1, dims).reshape(-1)).cuda()
+    ustar = torch.from_numpy(np.random.default_rng(2).normal(0.0, 1e-3, size=(npts, 3))).cuda()
+    eps0 = torch.from_numpy(problems.random_strain(0, dims, per)).cuda()
+
+    def run(prec, tol, ck):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        S = ProjectionSolver(dims, per, h, precision=prec, tol=tol, max_cycles=300, sweep_growth=False)
+        b0 = S.rhs_divergence(eps0).requires_grad_(True)
+        mu = mu0.clone().requires_grad_(True)
+        lam = (2 * mu0).clone().requires_grad_(True)
+        S.set_coefficients(mu, lam)
+
+        def inc(t):
+            g = torch.Generator(device="cuda")
+            g.manual_seed(3000 + t)
+            return S.rhs_divergence(torch.randn(ncells * 6, generator=g, dtype=torch.float64, device="cuda") * 1e-5)
+
+        torch.cuda.synchronize()
+        handle_bytes = free0 - torch.cuda.mem_get_info()[0]
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        t0 = time.perf_counter()
+        L = sequence_loss(S, b0, (T, inc), mu, lam, lambda t, u: ((u - ustar) ** 2).sum(), checkpoint_every=ck)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out = {"forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+               "peak_tensor_bytes": int(torch.cuda.max_memory_allocated() - base),
+               "solver_bytes": int(handle_bytes), "setups": S.stats["setups"],
+               "forward_cycles": S.stats["forward_cycles"],
+               "adjoint_cycles": S.stats["adjoint_cycles"], "loss": float(L.detach())}
+        grads = (b0.grad.detach().clone(), mu.grad.detach().clone(), lam.grad.detach().clone())
+        S.close()
+        return out, grads
+
+    mixed, g_mixed = run("mixed", TOL, every)
+    stored, _ = run("mixed", TOL, 0)
+    fp64, g_64 = run("fp64", 1e-12, every)
+    err = [float(torch.linalg.norm(a - r) / torch.linalg.norm(r)) for a, r in zip(g_mixed, g_64)]
+    line = {"metric": "50-solve sequence, forward/backward ms with checkpointing (256x256x257, mixed)",
+            "value": mixed["forward_ms"] + mixed["backward_ms"], "unit": "ms", "higher_is_better": False,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "50 warm-started solves, 256x256x257, h = 1/256, Lame operator, lognormal mu "
+                                   "(sigma 0.3, seed 1), lambda = 2 mu, b_t = b_{t-1} + div(N(0,1e-5) strain rate, "
+                                   "seeds 3000+t), loss sum_t |u_t - u*|^2, u* ~ N(0,1e-3) seed 2",
+                       "checkpoint_every": every},
+            "mixed_checkpointed": mixed, "mixed_stored": stored, "fp64_checkpointed": fp64,
+            "gradient_rel_err_vs_fp64": {"b0": err[0], "mu": err[1], "lam": err[2]}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, choices=[2, 3, 5], default=2,
+                    help="2: the 256x256x257 headline solve (default); 3: 512x512x257 variable mu, mixed vs FP64; "
+                         "5: 50-solve sequence with checkpointed backward")
     args = ap.parse_args()
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.config == 3 and args.impl == "ours":
+        run_config3(args, local)
+    elif args.config == 5 and args.impl == "ours":
+        run_config5(args, local)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_ours(args, world, rank, local)

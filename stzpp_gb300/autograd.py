@@ -65,21 +65,39 @@ class ProjectionSolver:
     def close(self):
         self.mg.close()
 
+    @staticmethod
+    def _tag(t):
+        return (t.data_ptr(), tuple(t.shape), tuple(t.stride()), t._version)
+
     def set_coefficients(self, mu, lam):
-        # the cached tensors are held, so a new tensor can never alias one of
-        # them (a freed address is reused by the caching allocator)
+        # The cached tensors are held, so their memory cannot be freed and
+        # handed to another tensor: a tensor with the same address, layout and
+        # version counter is then a view of the same, unmodified data (the
+        # saved-tensor copies autograd and checkpointing hand back are such
+        # views).
         if self._key is not None:
-            mu0, v0, lam0, w0 = self._key
-            if mu is mu0 and lam is lam0 and mu._version == v0 and lam._version == w0:
+            _, tm, _, tl = self._key
+            if self._tag(mu) == tm and self._tag(lam) == tl:
                 return
         torch.cuda.current_stream(self.device).synchronize()
         self.mg.setup_matrices(mu=mu.detach().contiguous(), lam=lam.detach().contiguous(), spacing=self.spacing,
                                dt=self.dt)
-        self._key = (mu, mu._version, lam, lam._version)
+        self._key = (mu, self._tag(mu), lam, self._tag(lam))
         self.stats["setups"] += 1
 
     def __call__(self, b, mu, lam, x0=None):
         return ProjectionSolve.apply(b, mu, lam, self, x0)
+
+    def rhs_divergence(self, eps):
+        """Node divergence of a cell tensor field (6 components per cell, a
+        float64 CUDA tensor), assembled on the device by the solver's kernel
+        (the r_field of shear_sim_3d); returns a new (npts, 3) tensor.  Uses
+        the handle's right-hand side as scratch."""
+        torch.cuda.current_stream(self.device).synchronize()
+        self.mg.set_rhs_divergence(eps.detach().contiguous(), self.spacing)
+        out = torch.empty((self.npts, 3), dtype=torch.float64, device=self.device)
+        self.mg.get_rhs(out)
+        return out
 
 
 def _check_field(t, shape, name):
@@ -133,6 +151,9 @@ def sequence_loss(solver, b0, increments, mu, lam, loss_fn, checkpoint_every=10,
     """Sum over t of loss_fn(t, u_t) for the chain of solves
     A u_t = b_t, b_t = b_{t-1} + increments[t-1] (t = 1..T), b_0 given, each
     solve warm-started from u_{t-1} (the start guess carries no gradient).
+    ``increments`` is a sequence of (npts, 3) tensors, or a pair (T, f) with
+    f(t) returning increment t (0-based) -- regenerated, not stored, when a
+    checkpointed segment is recomputed; f must be deterministic.
 
     Solves are grouped into segments of ``checkpoint_every``; each segment
     runs under ``torch.utils.checkpoint`` (non-reentrant), so the backward
@@ -140,7 +161,10 @@ def sequence_loss(solver, b0, increments, mu, lam, loss_fn, checkpoint_every=10,
     ``checkpoint_every`` <= 0 stores everything."""
     from torch.utils.checkpoint import checkpoint
 
-    T = len(increments)
+    if isinstance(increments, tuple) and len(increments) == 2 and callable(increments[1]):
+        T, inc = increments
+    else:
+        T, inc = len(increments), increments.__getitem__
     total = torch.zeros((), dtype=torch.float64, device=b0.device)
     b = b0
     x0 = None
@@ -149,7 +173,7 @@ def sequence_loss(solver, b0, increments, mu, lam, loss_fn, checkpoint_every=10,
         bb, xx = b_in, x_start
         part = torch.zeros((), dtype=torch.float64, device=b_in.device)
         for t in range(t0, t1):
-            bb = bb + increments[t]
+            bb = bb + inc(t)
             u = solver(bb, mu_, lam_, xx if warm_start else None)
             part = part + loss_fn(t + 1, u)
             xx = u.detach()
