@@ -1271,6 +1271,11 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
                 if (mixed) launch = [&] { launch_gs_colour<float>(h->op32[level], g, 0, h->L32[level].r, h->L32[level].x, h->st); };
                 else launch = [&] { launch_gs_colour<double>(h->op64[level], g, 0, h->L64[level].r, h->L64[level].x, h->st); };
                 break;
+            case STZ_MG_K_GS_SWEEP:
+                work = (9 * s + coef_bytes(level)) * npts_l;
+                if (mixed) launch = [&] { launch_gs_sweep<float>(h->op32[level], g, h->L32[level].r, h->L32[level].x, h->st); };
+                else launch = [&] { launch_gs_sweep<double>(h->op64[level], g, h->L64[level].r, h->L64[level].x, h->st); };
+                break;
             case STZ_MG_K_RESIDUAL:
                 work = (9 * s + coef_bytes(level)) * npts_l;
                 if (mixed) launch = [&] { launch_residual<float, float>(h->op32[level], g, h->L32[level].r, h->L32[level].x, h->L32[level].res, nullptr, nullptr, h->st); };

@@ -44,7 +44,7 @@ EXPORTS = (
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
-K_GS_COLOUR, K_RESIDUAL, K_RESTRICT, K_INTERP, K_RESIDUAL64 = range(5)
+K_GS_COLOUR, K_RESIDUAL, K_RESTRICT, K_INTERP, K_RESIDUAL64, K_GS_SWEEP = range(6)
 
 
 class StzMgError(RuntimeError):

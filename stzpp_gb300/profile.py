@@ -4,7 +4,8 @@
 
 sets up the 256x256x257 projection problem (the benchmark workload, or
 --dims), then launches the chosen kernel 3 + reps times through
-stz_mg_time_kernel and prints its time per launch and achieved bandwidth.
+stz_mg_time_kernel and prints its time per launch and achieved bandwidth
+("sweep" is a whole 8-colour smoother sweep, several launches).
 With --reps 1 the kernel of interest is the 4th launch of its name after
 setup, which makes ``ncu -k regex:<name> -s 3 -c 1`` capture exactly it.
 """
@@ -18,8 +19,8 @@ from . import mg as _mg
 from . import problems
 from .mg import Multigrid, elastic_stencil
 
-KERNELS = {"gs": _mg.K_GS_COLOUR, "residual": _mg.K_RESIDUAL, "restrict": _mg.K_RESTRICT,
-           "interp": _mg.K_INTERP, "residual64": _mg.K_RESIDUAL64}
+KERNELS = {"gs": _mg.K_GS_COLOUR, "sweep": _mg.K_GS_SWEEP, "residual": _mg.K_RESIDUAL,
+           "restrict": _mg.K_RESTRICT, "interp": _mg.K_INTERP, "residual64": _mg.K_RESIDUAL64}
 
 
 def main():

@@ -172,3 +172,4 @@ def test_reference_hierarchy_gs_bottom(oracle_port):
         ref.v_cycle(bottom="gs", smoother="mc8")
     assert rel_max(mg.get_x(), ref.get_field(0, "x")) < 1e-11
     mg.close()
+
