@@ -182,7 +182,7 @@ enum {
     STZ_MG_K_RESTRICT = 2,    /* restriction into `level` */
     STZ_MG_K_INTERP = 3,      /* interpolation from `level` */
     STZ_MG_K_RESIDUAL64 = 4,  /* FP64 top-level residual of the defect correction */
-    STZ_MG_K_GS_SWEEP = 5     /* one full 8-colour smoother sweep of a level */
+    STZ_MG_K_GS_SWEEP = 5     /* two full smoother sweeps of a level (one smoothing step of the cycle) */
 };
 int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
                        double *work_per_launch);

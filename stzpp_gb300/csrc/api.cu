@@ -543,7 +543,7 @@ void bottom_solve(stz_mg_handle h, Hier<T> H) {
     if (h->d.bottom == STZ_MG_BOTTOM_DIRECT) {
         launch_bottom_direct<T>(h->nbot_rows, h->ainv_t, h->nat_slot, g.npad, H.L[lb].r, H.L[lb].x, h->st);
     } else {
-        for (int s = 0; s < h->d.bottom_sweeps; s++) launch_gs_sweep<T>(H.op[lb], g, H.L[lb].r, H.L[lb].x, h->st);
+        launch_gs_sweeps<T>(H.op[lb], g, H.L[lb].r, H.L[lb].x, H.L[lb].res, h->d.bottom_sweeps, h->st);
     }
 }
 
@@ -581,8 +581,8 @@ void enqueue_vcycle(stz_mg_handle h, Hier<T> H) {
     const int lo = h->tail_lo >= 0 ? h->tail_lo : L - 1;
     for (int i = 0; i < lo; i++) {
         const Geom &g = h->geo[i];
-        for (int s = 0; s < h->d.v_down + (h->d.sweep_growth ? i : 0); s++)
-            launch_gs_sweep<T>(H.op[i], g, H.L[i].r, H.L[i].x, h->st);
+        launch_gs_sweeps<T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, h->d.v_down + (h->d.sweep_growth ? i : 0),
+                            h->st);
         launch_residual<T, T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, nullptr, nullptr, h->st);
         launch_restriction<T>(g, h->geo[i + 1], H.L[i].res, H.L[i + 1].r, h->st);
         CK(cudaMemsetAsync(H.L[i + 1].x, 0, 3 * (size_t)h->geo[i + 1].npad * sizeof(T), h->st));
@@ -596,8 +596,8 @@ void enqueue_vcycle(stz_mg_handle h, Hier<T> H) {
     if (h->tail_lo >= 0) CK(launch_tail_up<T>(td, h->tail_cluster, h->st));
     for (int i = lo; i > 0; i--) {
         launch_interpolation<T>(h->geo[i - 1], h->geo[i], H.L[i].x, H.L[i - 1].x, h->st);
-        for (int s = 0; s < h->d.v_up + (h->d.sweep_growth ? i - 1 : 0); s++)
-            launch_gs_sweep<T>(H.op[i - 1], h->geo[i - 1], H.L[i - 1].r, H.L[i - 1].x, h->st);
+        launch_gs_sweeps<T>(H.op[i - 1], h->geo[i - 1], H.L[i - 1].r, H.L[i - 1].x, H.L[i - 1].res,
+                            h->d.v_up + (h->d.sweep_growth ? i - 1 : 0), h->st);
     }
 }
 
@@ -1190,8 +1190,8 @@ int stz_mg_level_gauss_seidel(stz_mg_handle h, int level, int sweeps) {
     return guarded(h, [&] {
         need_setup(h);
         check_level(h, level);
-        for (int s = 0; s < sweeps; s++)
-            launch_gs_sweep<double>(h->op64[level], h->geo[level], h->L64[level].r, h->L64[level].x, h->st);
+        launch_gs_sweeps<double>(h->op64[level], h->geo[level], h->L64[level].r, h->L64[level].x, h->L64[level].res,
+                                 sweeps, h->st);
         sync(h);
     });
 }
@@ -1272,9 +1272,10 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
                 else launch = [&] { launch_gs_colour<double>(h->op64[level], g, 0, h->L64[level].r, h->L64[level].x, h->st); };
                 break;
             case STZ_MG_K_GS_SWEEP:
-                work = (9 * s + coef_bytes(level)) * npts_l;
-                if (mixed) launch = [&] { launch_gs_sweep<float>(h->op32[level], g, h->L32[level].r, h->L32[level].x, h->st); };
-                else launch = [&] { launch_gs_sweep<double>(h->op64[level], g, h->L64[level].r, h->L64[level].x, h->st); };
+                // two sweeps, as the V-cycle smooths (v_down = v_up = 2)
+                work = 2 * (9 * s + coef_bytes(level)) * npts_l;
+                if (mixed) launch = [&] { launch_gs_sweeps<float>(h->op32[level], g, h->L32[level].r, h->L32[level].x, h->L32[level].res, 2, h->st); };
+                else launch = [&] { launch_gs_sweeps<double>(h->op64[level], g, h->L64[level].r, h->L64[level].x, h->L64[level].res, 2, h->st); };
                 break;
             case STZ_MG_K_RESIDUAL:
                 work = (9 * s + coef_bytes(level)) * npts_l;

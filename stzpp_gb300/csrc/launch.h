@@ -24,6 +24,16 @@ template <typename T>
 void launch_gs_colour(const LevelOp<T> &op, const Geom &g, int q, const T *r, T *x, cudaStream_t st);
 template <typename T>
 void launch_gs_sweep(const LevelOp<T> &op, const Geom &g, const T *r, T *x, cudaStream_t st);
+// `sweeps` in-place sweeps of x; tmp (3*npad, may be null) lets large levels
+// use the tiled two-buffer sweep of tile.cu, with the same result
+template <typename T>
+void launch_gs_sweeps(const LevelOp<T> &op, const Geom &g, const T *r, T *x, T *tmp, int sweeps, cudaStream_t st);
+// tile.cu: one sweep reading xin and writing xout (levels periodic in x, y
+// with whole 32x32 tiles, shared-stencil or plane-invariant operators)
+template <typename T>
+bool gs_tile_applies(const LevelOp<T> &op, const Geom &g);
+template <typename T>
+void launch_gs_sweep_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st);
 int residual_blocks(const Geom &g);
 // res = r - A x (res may be null); when partial is non-null, per-block sums of
 // |res|^2 go to partial[residual_blocks(g)] and, when out is non-null, their

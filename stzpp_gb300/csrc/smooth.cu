@@ -314,14 +314,32 @@ void launch_gs_colour(const LevelOp<T> &op, const Geom &g, int q, const T *r, T 
     launch_gs_colour_planes(op, g, q, 0, g.O2, r, x, st);
 }
 
+// Large planes: one launch per colour keeps millions of threads in flight;
+// the plane-phase kernels (one block per plane) pay off where a colour of a
+// plane is at most two nodes per thread, i.e. where launch latency dominates.
+// (An odd periodic z would put both parities of a colour on one plane.)
+template <typename T>
+static bool large_planes(const Geom &g) {
+    const int phase_max = sizeof(T) == 8 ? 256 : 2 * kPhaseThreads;   // FP64 needs every SM's FP64 units
+    return (g.zp && (g.o & 1) && g.o > 1) || g.M2 * g.N2 > phase_max;
+}
+
+template <typename T>
+void launch_gs_sweeps(const LevelOp<T> &op, const Geom &g, const T *r, T *x, T *tmp, int sweeps, cudaStream_t st) {
+    int s = 0;
+    // pairs of sweeps x -> tmp -> x by the tiled kernel (tile.cu), which needs
+    // a second buffer; a last odd sweep in place (same result either way)
+    if (tmp && large_planes<T>(g) && gs_tile_applies(op, g))
+        for (; s + 2 <= sweeps; s += 2) {
+            launch_gs_sweep_tile(op, g, r, x, tmp, st);
+            launch_gs_sweep_tile(op, g, r, tmp, x, st);
+        }
+    for (; s < sweeps; s++) launch_gs_sweep(op, g, r, x, st);
+}
+
 template <typename T>
 void launch_gs_sweep(const LevelOp<T> &op, const Geom &g, const T *r, T *x, cudaStream_t st) {
-    // Large planes: one launch per colour keeps millions of threads in flight;
-    // the plane-phase kernels (one block per plane) pay off where a colour of a
-    // plane is at most two nodes per thread, i.e. where launch latency dominates.
-    // (An odd periodic z would put both parities of a colour on one plane.)
-    const int phase_max = sizeof(T) == 8 ? 256 : 2 * kPhaseThreads;   // FP64 needs every SM's FP64 units
-    if ((g.zp && (g.o & 1) && g.o > 1) || g.M2 * g.N2 > phase_max) {
+    if (large_planes<T>(g)) {
         for (int q = 0; q < 8; q++) launch_gs_colour(op, g, q, r, x, st);
         return;
     }
@@ -376,6 +394,10 @@ template void launch_gs_colour<float>(const LevelOp<float> &, const Geom &, int,
 template void launch_gs_colour<double>(const LevelOp<double> &, const Geom &, int, const double *, double *, cudaStream_t);
 template void launch_gs_sweep<float>(const LevelOp<float> &, const Geom &, const float *, float *, cudaStream_t);
 template void launch_gs_sweep<double>(const LevelOp<double> &, const Geom &, const double *, double *, cudaStream_t);
+template void launch_gs_sweeps<float>(const LevelOp<float> &, const Geom &, const float *, float *, float *, int,
+                                      cudaStream_t);
+template void launch_gs_sweeps<double>(const LevelOp<double> &, const Geom &, const double *, double *, double *, int,
+                                       cudaStream_t);
 template void launch_residual<float, float>(const LevelOp<float> &, const Geom &, const float *, const float *, float *, double *, double *, cudaStream_t);
 template void launch_residual<double, double>(const LevelOp<double> &, const Geom &, const double *, const double *, double *, double *, double *, cudaStream_t);
 template void launch_residual<double, float>(const LevelOp<double> &, const Geom &, const double *, const double *, float *, double *, double *, cudaStream_t);

@@ -5,7 +5,7 @@
 sets up the 256x256x257 projection problem (the benchmark workload, or
 --dims), then launches the chosen kernel 3 + reps times through
 stz_mg_time_kernel and prints its time per launch and achieved bandwidth
-("sweep" is a whole 8-colour smoother sweep, several launches).
+("sweep" is two whole 8-colour smoother sweeps, several launches).
 With --reps 1 the kernel of interest is the 4th launch of its name after
 setup, which makes ``ncu -k regex:<name> -s 3 -c 1`` capture exactly it.
 """

@@ -173,3 +173,53 @@ def test_reference_hierarchy_gs_bottom(oracle_port):
     assert rel_max(mg.get_x(), ref.get_field(0, "x")) < 1e-11
     mg.close()
 
+
+
+TILE_LEVEL_CASES = [((64, 64, 17), (True, True, False), 0, 2), ((64, 64, 16), (True, True, True), 0, 2),
+                    ((96, 64, 9), (True, True, False), 0, 4), ((128, 128, 17), (True, True, False), 1, 2),
+                    ((128, 128, 16), (True, True, True), 1, 3)]
+
+
+@pytest.mark.parametrize("dims,per,level,sweeps", TILE_LEVEL_CASES)
+def test_tiled_sweep_is_the_colour_sweep(dims, per, level, sweeps, monkeypatch):
+    """The tiled two-buffer sweep (each CTA runs a plane tile's four colours
+    from shared memory, recomputing a 4-node halo) gives bit-for-bit the
+    result of the eight colour launches: FP64 level sweeps of the shared
+    stencil and of a plane-invariant coarse operator, Dirichlet and periodic
+    z, even and odd sweep counts."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz)
+    out = {}
+    for tile in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_TILE", tile)
+        with sg.Multigrid(dims, per, precision="fp64", bottom="gs", max_coarse=5000) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            N = mg.level_npts(level)
+            rng = np.random.default_rng(8)
+            mg.level_set_field(level, "x", rng.standard_normal((N, 3)))
+            mg.level_set_field(level, "r", rng.standard_normal((N, 3)))
+            mg.gauss_seidel(level, sweeps)
+            out[tile] = mg.level_get_field(level, "x")
+    assert np.array_equal(out["0"], out["1"])
+
+
+def test_tiled_sweep_mixed_solve_bitwise(monkeypatch):
+    """The FP32 V-cycles of the mixed solve with and without the tiled sweep
+    give the same cycle count and the same solution bit for bit."""
+    import stzpp_gb300 as sg
+    dims, per = (128, 128, 33), (True, True, False)
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per, h=1.0 / 128)   # isotropic: the cycle converges
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    out = {}
+    for tile in ("0", "1"):   # 1: the tiled sweep on every level it applies to
+        monkeypatch.setenv("STZ_MG_TILE", tile)
+        with sg.Multigrid(dims, per, precision="mixed", sweep_growth=False) as mg:
+            mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, *h))
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-10, 100)
+            out[tile] = (cyc, mg.get_x())
+    assert out["0"][0] == out["1"][0]
+    assert np.array_equal(out["0"][1], out["1"][1])
