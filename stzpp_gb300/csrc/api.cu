@@ -290,6 +290,44 @@ __global__ void finite_check_kernel(const double *__restrict__ v, size_t n, int 
     for (; t < n; t += (size_t)gridDim.x * blockDim.x)
         if (!(v[t] - v[t] == 0.0)) { atomicExch(bad, 1); return; }
 }
+
+// flag[0] = 1 if any of v[0..n) is not zero
+__global__ void nonzero_kernel(const double *__restrict__ v, size_t n, int *flag) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; t < n; t += (size_t)gridDim.x * blockDim.x)
+        if (v[t] != 0.0) { atomicExch(flag, 1); return; }
+}
+
+// Sum of squares of v[0..n): one partial per block (fixed grid, fixed order),
+// then one block sums the partials -- deterministic.
+__global__ void sumsq_partial_kernel(const double *__restrict__ v, size_t n, double *__restrict__ partial) {
+    __shared__ double red[8];
+    double s = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        s += v[t] * v[t];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < blockDim.x / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
+__global__ void sum_blocks_kernel(const double *__restrict__ partial, int nb, double *__restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) s += partial[t];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = red[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) out[0] = s;
+    }
+}
 }  // namespace stzmg
 
 namespace {
@@ -665,14 +703,14 @@ double top_residual_sq(stz_mg_handle h, float *r32) {
     return v;
 }
 
+// |b|_2 of the top level, cached until the right-hand side changes: a plain
+// sum of squares over the field (the slots of no node hold zero).
 double rhs_norm(stz_mg_handle h) {
     if (h->bnorm < 0) {
-        // |b| via the residual kernel with x = 0 is wasteful; use a dedicated pass
         const Geom &g = h->geo[0];
-        double *zero = h->L64[0].res;
-        CK(cudaMemsetAsync(zero, 0, 3 * (size_t)g.npad * sizeof(double), h->st));
-        launch_residual<double, double>(h->op64[0], g, h->L64[0].r, zero, (double *)nullptr, h->partial, h->dscal,
-                                        h->st);
+        const int nb = std::min(h->partial_len, 4 * 152);
+        sumsq_partial_kernel<<<nb, 256, 0, h->st>>>(h->L64[0].r, 3 * (size_t)g.npad, h->partial);
+        sum_blocks_kernel<<<1, 1024, 0, h->st>>>(h->partial, nb, h->dscal);
         check_launch();
         CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
         sync(h);
@@ -680,6 +718,21 @@ double rhs_norm(stz_mg_handle h) {
         if (!std::isfinite(h->bnorm)) fail(STZ_MG_ERR_NONFINITE, "right-hand side is not finite");
     }
     return h->bnorm;
+}
+
+// Whether the top-level x is zero (the usual start of a solve): then b - A x
+// is b and the first FP64 residual pass is not needed.
+bool top_x_is_zero(stz_mg_handle h) {
+    const size_t n = 3 * (size_t)h->geo[0].npad;
+    CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+    const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
+    nonzero_kernel<<<blocks, 256, 0, h->st>>>(h->L64[0].x, n, h->dflag);
+    check_launch();
+    h->stat_launches += 1;
+    int flag = 1;
+    CK(cudaMemcpyAsync(&flag, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    sync(h);
+    return flag == 0;
 }
 
 // One mixed-precision defect-correction step with k FP32 V-cycles:
@@ -701,10 +754,11 @@ void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double 
     h->stat_launches = 0;
     const double bn = rhs_norm(h);
     const double target = tol * (bn > 0 ? bn : 1.0);
+    const bool x_zero = top_x_is_zero(h);
     int cycles = 0;
     double rsq;
     if (h->d.precision == STZ_MG_FP64) {
-        rsq = top_residual_sq(h, nullptr);
+        rsq = x_zero ? bn * bn : top_residual_sq(h, nullptr);
         while (std::sqrt(rsq) > target && cycles < max_cycles) {
             run_vcycle64(h, 1);
             cycles++;
@@ -715,7 +769,14 @@ void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double 
         // the number of cycles per step follows the observed contraction so
         // that each step gains about five digits (the FP32 floor) or reaches
         // the tolerance.
-        rsq = top_residual_sq(h, h->L32[0].r);
+        if (x_zero) {   // the correction's right-hand side is b itself
+            launch_convert(h->L64[0].r, h->L32[0].r, 3 * (size_t)h->geo[0].npad, h->st);
+            check_launch();
+            h->stat_launches += 1;
+            rsq = bn * bn;
+        } else {
+            rsq = top_residual_sq(h, h->L32[0].r);
+        }
         double rn = std::sqrt(rsq), rho = 0.2;
         int k = 6;
         const bool trace = std::getenv("STZ_MG_TRACE") != nullptr;
