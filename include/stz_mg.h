@@ -107,6 +107,18 @@ int stz_mg_get_rhs(stz_mg_handle h, double *r, int where);
  * one fewer.  Dirichlet nodes get 0. */
 int stz_mg_set_rhs_divergence(stz_mg_handle h, const double *eps, double dx, double dy, double dz, int where);
 
+/* Projection-step stress update after the solve (shear_sim_3d::projection_step,
+ * shear_sim_3d.cpp:681-710): for every cell, the velocity derivatives of
+ * calculate_first_order_velocities (shear_sim_3d.cpp:901-916) from the
+ * handle's current solution x, the increment ds = dt (lam tr(grad u) I +
+ * mu (grad u + grad u^T)) added to the cell's stress sigma in place, and
+ * *proj_mag = sum over cells of sym_mat3::modsq(ds) (mat3.hh:338-340; may be
+ * NULL).  sigma holds 6 doubles per cell (s11 s12 s13 s22 s23 s33), cells as
+ * for stz_mg_set_rhs_divergence; constant lam, mu.  The plates' velocities are
+ * the solved ones (x = fix^-1 b on the Dirichlet nodes). */
+int stz_mg_stress_update(stz_mg_handle h, double *sigma, double lam, double mu, double dt, double dx, double dy,
+                         double dz, double *proj_mag, int where);
+
 /* multigrid::v_cycle (multigrid.cc:253-297).  In mixed precision one call is
  * one defect-correction step: FP64 residual, one FP32 V-cycle, FP64 update. */
 int stz_mg_vcycle(stz_mg_handle h);

@@ -242,3 +242,59 @@ def grid_spacing(m, n, o, periodic, h=None):
         return h, h, h
     cells = [m if periodic[0] else m - 1, n if periodic[1] else n - 1, o if periodic[2] else o - 1]
     return tuple(1.0 / c for c in cells)
+
+
+def stress_update(u, sigma, lam, mu, dt, dx, dy, dz, dims, periodic):
+    """The projection-step stress update of the reference
+    (src/shear_sim_3d.cpp:681-710) with the velocity derivatives of
+    calculate_first_order_velocities (src/shear_sim_3d.cpp:901-916), evaluated
+    in the same order: returns (sigma + ds, per-cell sym_mat3::modsq(ds)
+    (src/mat3.hh:338-340)).  u: (npts, 3) node velocities in natural order
+    (the solution, plates included); sigma: (cells_z, cells_y, cells_x, 6)."""
+    m, n, o = dims
+    xp, yp, zp = periodic
+    oc, nc, mc, _ = sigma.shape
+    U = u.reshape(o, n, m, 3)
+
+    def node(c, di, dj, dk):
+        ks = (np.arange(oc) + dk) % o
+        js = (np.arange(nc) + dj) % n
+        is_ = (np.arange(mc) + di) % m
+        return U[np.ix_(ks, js, is_)][..., c]
+
+    qx, qy, qz = .25 * (1.0 / dx), .25 * (1.0 / dy), .25 * (1.0 / dz)
+
+    def ddx(c):
+        s = node(c, 1, 0, 0) - node(c, 0, 0, 0)
+        s = s + node(c, 1, 1, 0) - node(c, 0, 1, 0)
+        s = s + node(c, 1, 0, 1) - node(c, 0, 0, 1)
+        s = s + node(c, 1, 1, 1) - node(c, 0, 1, 1)
+        return qx * s
+
+    def ddy(c):
+        s = node(c, 0, 1, 0) - node(c, 0, 0, 0)
+        s = s + node(c, 1, 1, 0) - node(c, 1, 0, 0)
+        s = s + node(c, 0, 1, 1) - node(c, 0, 0, 1)
+        s = s + node(c, 1, 1, 1) - node(c, 1, 0, 1)
+        return qy * s
+
+    def ddz(c):
+        s = node(c, 0, 0, 1) - node(c, 0, 0, 0)
+        s = s + node(c, 1, 0, 1) - node(c, 1, 0, 0)
+        s = s + node(c, 0, 1, 1) - node(c, 0, 1, 0)
+        s = s + node(c, 1, 1, 1) - node(c, 1, 1, 0)
+        return qz * s
+
+    du_dx, du_dy, du_dz = ddx(0), ddy(0), ddz(0)
+    dv_dx, dv_dy, dv_dz = ddx(1), ddy(1), ddz(1)
+    dw_dx, dw_dy, dw_dz = ddx(2), ddy(2), ddz(2)
+    ds11 = dt * (lam * (dw_dz + dv_dy) + (lam + 2 * mu) * du_dx)
+    ds12 = dt * mu * (du_dy + dv_dx)
+    ds13 = dt * mu * (du_dz + dw_dx)
+    ds22 = dt * (lam * (dw_dz + du_dx) + (lam + 2 * mu) * dv_dy)
+    ds23 = dt * mu * (dv_dz + dw_dy)
+    ds33 = dt * (lam * (dv_dy + du_dx) + (lam + 2 * mu) * dw_dz)
+    ds = np.stack([ds11, ds12, ds13, ds22, ds23, ds33], axis=-1)
+    modsq = 0.5 * (ds11 * ds11 + ds12 * ds12 + ds13 * ds13 + ds12 * ds12 + ds22 * ds22 + ds23 * ds23
+                   + ds13 * ds13 + ds23 * ds23 + ds33 * ds33)
+    return sigma + ds, modsq

@@ -1027,6 +1027,32 @@ int stz_mg_set_rhs_divergence(stz_mg_handle h, const double *eps, double dx, dou
     });
 }
 
+int stz_mg_stress_update(stz_mg_handle h, double *sigma, double lam, double mu, double dt, double dx, double dy,
+                         double dz, double *proj_mag, int where) {
+    if (!h || !sigma) return set_error(STZ_MG_ERR_ARG, "null argument");
+    if (!(dx > 0 && dy > 0 && dz > 0)) return set_error(STZ_MG_ERR_ARG, "bad spacing");
+    if (where != STZ_MG_HOST && where != STZ_MG_DEVICE)
+        return set_error(STZ_MG_ERR_ARG, "where must be STZ_MG_HOST or STZ_MG_DEVICE");
+    return guarded(h, [&] {
+        const Geom &g = h->geo[0];
+        const size_t ncells = (size_t)(g.xp ? g.m : g.m - 1) * (g.yp ? g.n : g.n - 1) * (g.zp ? g.o : g.o - 1);
+        double *dsig = sigma;
+        if (where == STZ_MG_HOST) {
+            dsig = staging(h, 6 * ncells);
+            CK(cudaMemcpyAsync(dsig, sigma, 6 * ncells * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        }
+        const int nb = std::min(h->partial_len, 4 * 152);
+        launch_stress_update(g, h->L64[0].x, dsig, lam, mu, dt, dx, dy, dz, h->partial, nb, h->st);
+        sum_blocks_kernel<<<1, 1024, 0, h->st>>>(h->partial, nb, h->dscal);
+        check_launch();
+        if (where == STZ_MG_HOST)
+            CK(cudaMemcpyAsync(sigma, dsig, 6 * ncells * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        if (proj_mag) *proj_mag = h->hscal[0];
+    });
+}
+
 int stz_mg_vcycle(stz_mg_handle h) {
     if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
     return guarded(h, [&] {

@@ -75,6 +75,11 @@ void launch_gauss_jordan(double *aug, int n, double *inv, int *piv, double *col,
 // r (colour-blocked, 3 x npad) = node divergence of the cell tensor field eps
 void launch_rhs_divergence(const Geom &g, const double *eps, double dx, double dy, double dz, double *r,
                            cudaStream_t st);
+// sigma (6 doubles per cell, natural order) += the projection-step stress
+// increment of the solution u (colour-blocked FP64); per-block sums of
+// modsq(increment) to partial[0 .. nblocks)
+void launch_stress_update(const Geom &g, const double *u, double *sigma, double lam, double mu, double dt, double dx,
+                          double dy, double dz, double *partial, int nblocks, cudaStream_t st);
 
 // adjoint.cu (natural-order vec3 fields, 3 doubles per node)
 // dst = src with the rows of Dirichlet nodes zeroed

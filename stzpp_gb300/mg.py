@@ -40,7 +40,7 @@ EXPORTS = (
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
     "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
-    "stz_mg_adjoint_solve", "stz_mg_coeff_grad",
+    "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update",
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
@@ -103,6 +103,7 @@ def load_library():
     lib.stz_mg_const_residual_sumsq_noalloc.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, ci, vp]
     lib.stz_mg_adjoint_solve.argtypes = [vp, vp, vp, ci, cd, ci, ctypes.POINTER(ci), ctypes.POINTER(cd)]
     lib.stz_mg_coeff_grad.argtypes = [vp, vp, vp, vp, vp, ci]
+    lib.stz_mg_stress_update.argtypes = [vp, vp, cd, cd, cd, cd, cd, cd, ctypes.POINTER(cd), ci]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci
@@ -288,6 +289,25 @@ class Multigrid:
         p, where, keep = _arg(out, 3 * self.npts)
         _check(load_library().stz_mg_get_x(self._h, p, where))
         return out
+
+    def stress_update(self, sigma, lam, mu, dt, spacing):
+        """Projection-step stress update (shear_sim_3d.cpp:681-710) from the
+        current solution: sigma (6 per cell, a float64 numpy array or CUDA
+        tensor) is updated in place; returns proj_mag."""
+        m, n, o = self.dims
+        xp, yp, zp = self.periodic
+        ncells = (m if xp else m - 1) * (n if yp else n - 1) * (o if zp else o - 1)
+        if hasattr(sigma, "is_cuda") and sigma.is_cuda:
+            p, where, keep = _arg(sigma, 6 * ncells)
+        else:
+            if not (isinstance(sigma, np.ndarray) and sigma.dtype == np.float64 and sigma.flags.c_contiguous):
+                raise ValueError("sigma must be a contiguous float64 array (updated in place)")
+            if sigma.size != 6 * ncells:
+                raise ValueError(f"expected {6 * ncells} elements, got {sigma.size}")
+            p, where = sigma.ctypes.data_as(ctypes.c_void_p), HOST
+        pm = ctypes.c_double()
+        _check(load_library().stz_mg_stress_update(self._h, p, lam, mu, dt, *spacing, ctypes.byref(pm), where))
+        return pm.value
 
     # --------------------------------------------------------------- solve
     def v_cycle(self):
