@@ -224,7 +224,8 @@ def run_ours(args, world, rank, local):
         return reduce_max(v, dist, "cuda" if dist is None or dist.get_backend() == "nccl" else "cpu")
 
     # ---------------------------------------------------------- mixed solve
-    mg = sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, device=local, stream=stream.cuda_stream)
+    mg = sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, max_coarse=args.max_coarse, device=local,
+                      stream=stream.cuda_stream)
     t0 = time.perf_counter()
     mg.setup_matrices(stencil=stencil, fix=fix)
     torch.cuda.synchronize()
@@ -299,7 +300,8 @@ def run_ours(args, world, rank, local):
     mg.close()
 
     # ------------------------------------------------------ FP64 solve
-    mg64 = sg.Multigrid(dims, per, precision="fp64", sweep_growth=False, device=local, stream=stream.cuda_stream)
+    mg64 = sg.Multigrid(dims, per, precision="fp64", sweep_growth=False, max_coarse=args.max_coarse, device=local,
+                        stream=stream.cuda_stream)
     mg64.setup_matrices(stencil=stencil, fix=fix)
     mg64.set_rhs(b_dev)
     steps64 = max(2, args.steps // 2)
@@ -325,7 +327,8 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "dims": list(dims), "precision": "mixed: FP32 V-cycles, FP64 residual/update/bottom",
-                       "cycle": "V(2,2) on every level, 8-colour block GS, RAT coarse operators (plane-invariant storage), FP64 direct solve at 8x8x9",
+                       "cycle": ("V(2,2) on every level, 8-colour block GS, RAT coarse operators (plane-invariant "
+                                 f"storage), FP64 direct solve of the coarsest level (<= {args.max_coarse} nodes)"),
                        "replicas": world, "l2": "inputs larger than L2 (fine vectors 404 MB each); no flush needed"},
             "cycles": cycles, "relres": rel, "setup_ms": setup_ms,
             "fp64": {"ms_per_solve": ms_fp64, "cycles": cyc64, "relres": rel64},
@@ -479,21 +482,77 @@ def run_config5(args, local, T=50, every=10):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ coefficient change
+def run_coeff_change(args, local, steps=12):
+    """The trans_sim per-step path: each step uploads a new transformed-frame
+    shared stencil (the reference's own stencils of trans_sim_3d for three
+    frames, tests/golden/trans_stencils.npz, cycled), rebuilds the hierarchy
+    (RAT + bottom inverse), and solves the 256x256x257 projection to 1e-10 in
+    mixed precision warm-started from the previous step."""
+    import torch
+    torch.cuda.set_device(local)
+    import stzpp_gb300 as sg
+    from stzpp_gb300 import problems
+    dims, per = DIMS, PERIODIC
+    h = 1.0 / 256
+    d = np.load(os.path.join(ROOT, "tests", "golden", "trans_stencils.npz"))
+    frames = [(d["stencil"][c].reshape(27, 9) / (h * h), d["fix"][c] / (h * h)) for c in range(len(d["T"]))]
+    stream = torch.cuda.current_stream()
+    out = {}
+    for mc in (1024, 16):
+        mg = sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, max_coarse=mc, device=local,
+                          stream=stream.cuda_stream)
+        mg.setup_matrices(*frames[0])
+        mg.set_rhs_divergence(problems.random_strain(0, dims, per), (h, h, h))
+        mg.set_x(np.zeros(3 * mg.npts))
+        t_set, t_solve, cyc = [], [], []
+        for s in range(steps + 2):
+            st, fix = frames[s % len(frames)]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mg.setup_matrices(stencil=st, fix=fix)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            c, rel = mg.solve(TOL, 300)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            if s >= 2:
+                t_set.append((t1 - t0) * 1e3)
+                t_solve.append((t2 - t1) * 1e3)
+                cyc.append(c)
+        out[f"max_coarse_{mc}"] = {"levels": mg.nlevels, "setup_ms": statistics.median(t_set),
+                                   "solve_ms": statistics.median(t_solve), "cycles": cyc,
+                                   "step_ms": statistics.median([a + b for a, b in zip(t_set, t_solve)])}
+        mg.close()
+    line = {"metric": "ms per coefficient-change step (new shared stencil + set-up + solve to 1e-10), 256x256x257 mixed",
+            "value": out["max_coarse_16"]["step_ms"], "unit": "ms", "higher_is_better": False, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "256x256x257, h = 1/256, the reference's trans_sim_3d stencils for 3 frames "
+                                   "(full non-symmetric 3x3 blocks), cycled; RHS = divergence of N(0,1e-3) strain "
+                                   "(seed 0); each solve warm-started from the previous step", "steps": steps},
+            **out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", type=int, choices=[2, 3, 5], default=2,
+    ap.add_argument("--config", type=int, choices=[2, 3, 5, 6], default=2,
                     help="2: the 256x256x257 headline solve (default); 3: 512x512x257 variable mu, mixed vs FP64; "
-                         "5: 50-solve sequence with checkpointed backward")
+                         "5: 50-solve sequence with checkpointed backward; 6: per-step coefficient change")
+    ap.add_argument("--max-coarse", type=int, default=1024,
+                    help="hierarchy stop rule of the headline solve (reference: 1024 nodes)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.config == 3 and args.impl == "ours":
         run_config3(args, local)
     elif args.config == 5 and args.impl == "ours":
         run_config5(args, local)
+    elif args.config == 6 and args.impl == "ours":
+        run_coeff_change(args, local)
     elif args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -70,7 +71,8 @@ struct ApiError {
 template <typename T>
 struct Level {
     T *x = nullptr, *r = nullptr, *res = nullptr;   // 3*npad each
-    T *coef = nullptr, *dinv = nullptr;             // dense levels
+    T *coef = nullptr, *dinv = nullptr;             // coarse operators (243 and 9 per row)
+    size_t coef_rows = 0;                           // rows coef / dinv were allocated for
 };
 
 constexpr int kMaxLev = kMaxLevels;
@@ -97,6 +99,10 @@ struct stz_mg_handle_s {
     double *ainv_t = nullptr;
     int *nat_slot = nullptr;
     int nbot_rows = 0;
+    // set-up scratch kept between set-ups (a coefficient change re-runs set-up)
+    double *bot_aug = nullptr, *bot_col = nullptr, *bot_dense = nullptr;
+    int *bot_piv = nullptr, *bot_S = nullptr;
+    size_t bot_aug_len = 0, bot_dense_len = 0, bot_S_len = 0;
     // scratch
     double *partial = nullptr;
     int partial_len = 0;
@@ -123,6 +129,14 @@ struct stz_mg_handle_s {
         CK(cudaMalloc(&p, n * sizeof(T) ? n * sizeof(T) : 1));
         allocs.push_back(p);
         return (T *)p;
+    }
+    // p holds at least n elements afterwards (reallocated only to grow)
+    template <typename T>
+    void ensure(T *&p, size_t &cap, size_t n) {
+        if (p && cap >= n) return;
+        release(p);
+        p = alloc<T>(n);
+        cap = n;
     }
     void release(void *p) {
         if (!p) return;
@@ -353,12 +367,11 @@ void build_bottom(stz_mg_handle h) {
     // dense operator of the bottom level, natural order
     std::vector<double> Anat(243 * N);
     {
-        double *dcoef = nullptr;
         const double *src = nullptr;
         if (h->op64[lb].kind != OP_DENSE) {
-            dcoef = h->alloc<double>(243 * (size_t)g.npad);
-            launch_expand_dense(h->op64[lb], g, dcoef, h->st);
-            src = dcoef;
+            h->ensure(h->bot_dense, h->bot_dense_len, 243 * (size_t)g.npad);
+            launch_expand_dense(h->op64[lb], g, h->bot_dense, h->st);
+            src = h->bot_dense;
         } else {
             src = h->op64[lb].dop.coef;
         }
@@ -367,16 +380,14 @@ void build_bottom(stz_mg_handle h) {
         check_launch();
         CK(cudaMemcpyAsync(Anat.data(), nat, 243 * N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         sync(h);
-        h->release(dcoef);
     }
     std::vector<int> Snat(6 * N);
     {
-        int *tmp = h->alloc<int>(6 * N);
-        launch_bounds_cb_to_nat(g, h->S[lb], tmp, h->st);
+        h->ensure(h->bot_S, h->bot_S_len, 6 * N);
+        launch_bounds_cb_to_nat(g, h->S[lb], h->bot_S, h->st);
         check_launch();
-        CK(cudaMemcpyAsync(Snat.data(), tmp, 6 * N * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(Snat.data(), h->bot_S, 6 * N * sizeof(int), cudaMemcpyDeviceToHost, h->st));
         sync(h);
-        h->release(tmp);
     }
     std::vector<double> M((size_t)nr * nr, 0.0);
     auto wrap = [](int a, int len) { a %= len; return a < 0 ? a + len : a; };
@@ -407,31 +418,33 @@ void build_bottom(stz_mg_handle h) {
         std::memcpy(&aug[(size_t)r * 2 * nr], &M[(size_t)r * nr], nr * sizeof(double));
         aug[(size_t)r * 2 * nr + nr + r] = 1.0;
     }
-    double *daug = h->alloc<double>(aug.size());
-    double *dcol = h->alloc<double>(nr);
-    int *dpiv = h->alloc<int>(1);
-    h->release(h->ainv_t);
-    h->ainv_t = h->alloc<double>((size_t)nr * nr);
-    CK(cudaMemcpyAsync(daug, aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    // buffers are sized by the bottom level, which does not change between set-ups
+    if (!h->bot_aug || h->nbot_rows != nr) {
+        h->release(h->bot_aug);
+        h->release(h->bot_col);
+        h->release(h->bot_piv);
+        h->release(h->ainv_t);
+        h->release(h->nat_slot);
+        h->bot_aug = h->alloc<double>(aug.size());
+        h->bot_col = h->alloc<double>(nr);
+        h->bot_piv = h->alloc<int>(1);
+        h->ainv_t = h->alloc<double>((size_t)nr * nr);
+        h->nat_slot = h->alloc<int>(N);
+        std::vector<int> ns(N);
+        for (int k = 0; k < g.o; k++)
+            for (int j = 0; j < g.n; j++)
+                for (int i = 0; i < g.m; i++) ns[i + (size_t)g.m * (j + (size_t)g.n * k)] = slot(g, i, j, k);
+        CK(cudaMemcpyAsync(h->nat_slot, ns.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        h->nbot_rows = nr;
+    }
+    CK(cudaMemcpyAsync(h->bot_aug, aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
-    launch_gauss_jordan(daug, nr, h->ainv_t, dpiv, dcol, h->dflag, h->st);
+    launch_gauss_jordan(h->bot_aug, nr, h->ainv_t, h->bot_piv, h->bot_col, h->dflag, h->st);
     check_launch();
     int singular = 0;
     CK(cudaMemcpyAsync(&singular, h->dflag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     sync(h);
-    h->release(daug);
-    h->release(dcol);
-    h->release(dpiv);
     if (singular) fail(STZ_MG_ERR_SINGULAR, "bottom-level matrix is singular");
-    std::vector<int> ns(N);
-    for (int k = 0; k < g.o; k++)
-        for (int j = 0; j < g.n; j++)
-            for (int i = 0; i < g.m; i++) ns[i + (size_t)g.m * (j + (size_t)g.n * k)] = slot(g, i, j, k);
-    h->release(h->nat_slot);
-    h->nat_slot = h->alloc<int>(N);
-    CK(cudaMemcpyAsync(h->nat_slot, ns.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->st));
-    sync(h);
-    h->nbot_rows = nr;
 }
 
 // Levels small enough for the persistent cluster kernels: the first coarse
@@ -465,9 +478,28 @@ void choose_tail(stz_mg_handle h) {
     h->tail_cap_planes = cap;
 }
 
+// Wall time of set-up phases on stderr when STZ_MG_TRACE is set (the stream
+// is synchronised at each mark, so only for measurement).
+struct PhaseTrace {
+    stz_mg_handle h;
+    bool on;
+    std::chrono::steady_clock::time_point t0;
+    explicit PhaseTrace(stz_mg_handle hh) : h(hh), on(std::getenv("STZ_MG_TRACE") != nullptr) {
+        if (on) t0 = std::chrono::steady_clock::now();
+    }
+    void mark(const char *what) {
+        if (!on) return;
+        sync(h);
+        auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "stz_mg setup: %-22s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(t - t0).count());
+        t0 = t;
+    }
+};
+
 void setup(stz_mg_handle h) {
     if (h->top_kind < 0) fail(STZ_MG_ERR_ARG, "no operator: call stz_mg_set_stencil_const, _points or _coeffs_lame first");
     invalidate(h);
+    PhaseTrace trace(h);
     const bool mixed = h->d.precision == STZ_MG_MIXED;
     // top level: dense per-point operator needs its centre inverses
     if (h->top_kind == OP_DENSE) {
@@ -495,10 +527,13 @@ void setup(stz_mg_handle h) {
         const Geom &gf = h->geo[l - 1], &gc = h->geo[l];
         const size_t rows = plane ? (size_t)gc.o : (size_t)gc.npad;
         Level<double> &C = h->L64[l];
-        h->release(C.coef);
-        h->release(C.dinv);
-        C.coef = h->alloc<double>(243 * rows);
-        C.dinv = h->alloc<double>(9 * rows);
+        if (C.coef_rows != rows) {
+            h->release(C.coef);
+            h->release(C.dinv);
+            C.coef = h->alloc<double>(243 * rows);
+            C.dinv = h->alloc<double>(9 * rows);
+            C.coef_rows = rows;
+        }
         launch_rat_bounds(gf, h->S[l - 1], gc, h->S[l], h->dflag + 1, h->st);
         launch_rat(h->op64[l - 1], gf, gc, C.coef, plane, h->st);
         if (plane) launch_plane_dinv<double>(gc.o, C.coef, C.dinv, h->dflag, h->st);
@@ -540,10 +575,13 @@ void setup(stz_mg_handle h) {
         }
         if (mixed) {
             Level<float> &F = h->L32[l];
-            h->release(F.coef);
-            h->release(F.dinv);
-            F.coef = h->alloc<float>(243 * rows);
-            F.dinv = h->alloc<float>(9 * rows);
+            if (F.coef_rows != rows) {
+                h->release(F.coef);
+                h->release(F.dinv);
+                F.coef = h->alloc<float>(243 * rows);
+                F.dinv = h->alloc<float>(9 * rows);
+                F.coef_rows = rows;
+            }
             launch_convert(C.coef, F.coef, 243 * rows, h->st);
             launch_convert(C.dinv, F.dinv, 9 * rows, h->st);
             check_launch();
@@ -562,7 +600,9 @@ void setup(stz_mg_handle h) {
     sync(h);
     if (flags[1]) fail(STZ_MG_ERR_UNSUPPORTED, "RAT box bounds out of range");
     if (flags[0]) fail(STZ_MG_ERR_SINGULAR, "singular or non-finite diagonal block on a coarse level");
+    trace.mark("coarse operators (RAT)");
     if (h->d.bottom == STZ_MG_BOTTOM_DIRECT) build_bottom(h);
+    trace.mark("bottom inverse");
     choose_tail(h);
     h->setup_done = true;
 }

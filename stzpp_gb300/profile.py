@@ -31,16 +31,30 @@ def main():
     ap.add_argument("--level", type=int, default=0)
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--operator", default="const", choices=["const", "lame"])
+    ap.add_argument("--max-coarse", type=int, default=1024)
+    ap.add_argument("--setup", action="store_true",
+                    help="time the set-up after an operator change (stencil upload + RAT + bottom inverse) instead")
     args = ap.parse_args()
     dims = tuple(int(v) for v in args.dims.split("x"))
     per = (True, True, False)
     h = problems.grid_spacing(dims, per)
-    with Multigrid(dims, per, precision=args.precision) as m:
+    with Multigrid(dims, per, precision=args.precision, max_coarse=args.max_coarse) as m:
         if args.operator == "const":
             m.setup_matrices(*elastic_stencil(1.0, 2.0, *h))
         else:
             mu = problems.lognormal_mu(1, dims).reshape(-1)
             m.setup_matrices(mu=mu, lam=2 * mu, spacing=h)
+        if args.setup:
+            import time
+            st, fix = elastic_stencil(1.0, 2.0, *h)
+            times = []
+            for rep in range(max(2, args.reps)):
+                t0 = time.perf_counter()
+                m.setup_matrices(stencil=st * (1.0 + 1e-3 * rep), fix=fix * (1.0 + 1e-3 * rep))
+                times.append((time.perf_counter() - t0) * 1e3)
+            print(f"setup {args.precision} {args.dims} max_coarse {args.max_coarse} ({m.nlevels} levels): "
+                  f"{min(times[1:]):.1f} ms best, {sorted(times[1:])[len(times[1:]) // 2]:.1f} ms median")
+            return
         m.set_rhs_divergence(problems.random_strain(0, dims, per), h)
         m.set_x(np.zeros(3 * m.npts))
         ms, work = m.time_kernel(KERNELS[args.kernel], args.level, reps=args.reps)

@@ -19,7 +19,11 @@ Cases (all seeded):
 For each small case: box bounds S and coefficients of every level, one GS
 sweep, restriction, interpolation and two V-cycles from seeded fields.
 
-Run: python tests/golden/make_golden.py
+Also ``trans``: the reference's transformed-frame stencils of trans_sim_3d
+for a few frames (the coefficient-change path), from its generated
+stenc_funcs.hh -> tests/golden/trans_stencils.npz.
+
+Run: python tests/golden/make_golden.py [trans]
 """
 import os
 import sys
@@ -76,7 +80,37 @@ def small_case(out, name, dims, per, kind, max_coarse):
     R.close()
 
 
+# transforms of the trans_sim frame for the coefficient-change fixtures
+TRANS_T = [[[1.0, 0.0, 0.3], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]],
+           [[1.0, 0.0, 0.1], [0.0, 1.0, -0.2], [0.0, 0.0, 1.0]],
+           [[1.05, 0.02, 0.15], [0.0, 0.97, 0.05], [0.0, 0.0, 1.0]]]
+
+
+def trans_stencils(path):
+    """Stencils of trans_sim_3d::set_up_stencil_and_matrices for the TRANS_T
+    frames (mu = 1, lambda = 2, dt = 1, dx = dy = dz = 1), computed by the
+    reference's generated functions (oracle/trans_stencil.py builds them)."""
+    import ctypes
+    lib_path = os.path.join(ROOT, "oracle", "_ref", "libtransstencil.so")
+    if not os.path.exists(lib_path):
+        sys.exit("oracle/_ref/libtransstencil.so is missing: run `python oracle/trans_stencil.py <reference>/src`")
+    lib = ctypes.CDLL(lib_path)
+    lib.ref_trans_stencil.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [ctypes.c_void_p] * 2
+    T = np.array(TRANS_T)
+    S = np.zeros((len(T), 243))
+    F = np.zeros((len(T), 9))
+    for c in range(len(T)):
+        t = np.ascontiguousarray(T[c])
+        lib.ref_trans_stencil(t.ctypes.data_as(ctypes.c_void_p), 1.0, 2.0, 1.0, 1.0, 1.0, 1.0,
+                              S[c].ctypes.data_as(ctypes.c_void_p), F[c].ctypes.data_as(ctypes.c_void_p))
+    np.savez_compressed(path, T=T, stencil=S, fix=F)
+    print("wrote", path)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "trans":
+        trans_stencils(os.path.join(HERE, "trans_stencils.npz"))
+        return
     if not refpy.available():
         sys.exit("oracle/_ref/libstzref.so is missing: run `make -C oracle ref` where the reference is available")
     out = {}

@@ -22,11 +22,21 @@ SOLUTION_RTOL = 1e-9
 
 GRIDS = [
     ((16, 16, 17), (True, True, False), "const"),
+    ((16, 16, 17), (True, True, False), "trans"),
     ((16, 16, 17), (True, True, False), "points"),
     ((16, 16, 17), (True, True, False), "lame"),
     ((12, 10, 9), (False, False, False), "const"),
     ((16, 12, 10), (True, False, False), "const"),
 ]
+
+
+def trans_stencil(c, h):
+    """Frame c of the reference's transformed-frame stencils (trans_sim_3d,
+    golden fixture computed at dx = dy = dz = 1) on a grid of spacing h: a
+    full, non-symmetric shared stencil (the coefficient-change path)."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "trans_stencils.npz"))
+    return d["stencil"][c].reshape(27, 9) / (h * h), d["fix"][c] / (h * h)
 
 
 def rel_max(a, b):
@@ -43,6 +53,10 @@ def build_pair(dims, per, kind, oracle_port, max_coarse=16, precision="fp64", bo
         ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=max_coarse)
         st_gpu, fix_gpu = sg.elastic_stencil(1.0, 2.0, dx, dy, dz)
         mg.setup_matrices(stencil=st_gpu, fix=fix_gpu)
+    elif kind == "trans":
+        st, fix = trans_stencil(0, dx)
+        ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=max_coarse)
+        mg.setup_matrices(stencil=st, fix=fix)
     else:
         mu = P.lognormal_mu(1, m, n, o)
         pts = P.elastic_stencil_points(mu, 2 * mu, dx, dy, dz, per)
@@ -122,7 +136,7 @@ def test_vcycle_iterates(dims, per, kind, oracle_port):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("kind", ["const", "lame"])
+@pytest.mark.parametrize("kind", ["const", "lame", "trans"])
 def test_solution_matches_reference_solver(precision, kind, oracle_port):
     """32x32x33 (dx = 1/32), periodic x,y, Dirichlet z: converged solution of the
     GPU solve against the reference's lexicographic solver with its own
@@ -135,6 +149,9 @@ def test_solution_matches_reference_solver(precision, kind, oracle_port):
     if kind == "const":
         st, fix = P.elastic_stencil_const(1.0, 2.0, dx, dy, dz)
         ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=1024)
+    elif kind == "trans":
+        st, fix = trans_stencil(2, dx)
+        ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=1024)
     else:
         mu = P.lognormal_mu(1, m, n, o)
         ref = oracle_port.PortMultigrid(dims, per, points=P.elastic_stencil_points(mu, 2 * mu, dx, dy, dz, per),
@@ -146,6 +163,8 @@ def test_solution_matches_reference_solver(precision, kind, oracle_port):
     with sg.Multigrid(dims, per, precision=precision) as mg:
         if kind == "const":
             mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, dx, dy, dz))
+        elif kind == "trans":
+            mg.setup_matrices(stencil=st, fix=fix)
         else:
             mg.setup_matrices(mu=mu.reshape(-1), lam=(2 * mu).reshape(-1), spacing=(dx, dy, dz))
         mg.setup_fields(r=b)

@@ -212,3 +212,63 @@ def test_rhs_vanishes_on_dirichlet_nodes_and_sums_to_zero_in_periodic_dims():
     assert not b[0].any() and not b[-1].any()
     # the x-derivative terms telescope over a periodic x-row
     assert np.isfinite(b).all() and np.abs(b).max() > 0
+
+
+# ---------------------------------------------------------------- trans_sim frames
+TRANS = os.path.join(HERE, "golden", "trans_stencils.npz")
+
+
+def test_trans_fixture_matches_reference_functions():
+    """The golden transformed-frame stencils are what the reference's
+    generated functions give (oracle/trans_stencil.py harness), and the
+    identity frame is the shear_sim elasticity stencil."""
+    import ctypes
+    d = np.load(TRANS)
+    lib_path = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libtransstencil.so")
+    if os.path.exists(lib_path):
+        lib = ctypes.CDLL(lib_path)
+        lib.ref_trans_stencil.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [ctypes.c_void_p] * 2
+        for c in range(len(d["T"])):
+            t = np.ascontiguousarray(d["T"][c])
+            S, F = np.zeros(243), np.zeros(9)
+            lib.ref_trans_stencil(t.ctypes.data_as(ctypes.c_void_p), 1.0, 2.0, 1.0, 1.0, 1.0, 1.0,
+                                  S.ctypes.data_as(ctypes.c_void_p), F.ctypes.data_as(ctypes.c_void_p))
+            assert np.array_equal(S, d["stencil"][c]) and np.array_equal(F, d["fix"][c])
+        t = np.ascontiguousarray(np.eye(3))
+        S, F = np.zeros(243), np.zeros(9)
+        lib.ref_trans_stencil(t.ctypes.data_as(ctypes.c_void_p), 1.0, 2.0, 1.0, 1.0, 1.0, 1.0,
+                              S.ctypes.data_as(ctypes.c_void_p), F.ctypes.data_as(ctypes.c_void_p))
+        st, fix = P.elastic_stencil_const(1.0, 2.0, 1.0, 1.0, 1.0)
+        assert np.array_equal(S.reshape(27, 9), st) and np.array_equal(F, fix)
+    S = d["stencil"].reshape(-1, 27, 3, 3)
+    assert not any(np.allclose(S[c], np.swapaxes(S[c][::-1], 1, 2)) for c in range(len(S)))   # non-symmetric
+
+
+@pytest.mark.parametrize("frame", [0, 1, 2])
+def test_port_matches_live_reference_trans(frame, oracle_port):
+    """The C restatement against the compiled reference on a transformed-frame
+    (full, non-symmetric) shared stencil: coarse operators, sweeps, transfers
+    and V-cycles."""
+    from oracle import refpy
+    if not refpy.available():
+        pytest.skip("compiled reference not available on this machine")
+    dims, per = (16, 16, 17), (True, True, False)
+    h = 1.0 / 16
+    d = np.load(TRANS)
+    st, fix = d["stencil"][frame].reshape(27, 9) / (h * h), d["fix"][frame] / (h * h)
+    R = refpy.RefMultigrid(dims, per, stencil=st, fix=fix, max_coarse=16)
+    Q = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=16)
+    assert R.nlevels == Q.nlevels
+    rng = np.random.default_rng(frame)
+    for l in range(R.nlevels):
+        assert np.array_equal(R.level_S(l), Q.level_S(l))
+        assert rel(Q.level_A(l), R.level_A(l)) < 1e-13
+    x0 = rng.standard_normal((R.npts(0), 3))
+    b0 = rng.standard_normal((R.npts(0), 3))
+    for M in (R, Q):
+        M.set_field(0, "x", x0)
+        M.set_field(0, "r", b0)
+    for _ in range(2):
+        R.v_cycle("gs")
+        Q.v_cycle(bottom="gs", smoother="lex")
+    assert rel(Q.get_field(0, "x"), R.get_field(0, "x")) < 1e-11
