@@ -56,7 +56,6 @@ __device__ void lame_block(const LameOp<double> &op, const Geom &g, int i, int j
 #pragma unroll
     for (int e = 0; e < 9; e++) blk[e] = 0.0;
     const int nz = (d[0] != 0) + (d[1] != 0) + (d[2] != 0);
-    const double hh[3] = {op.dx, op.dy, op.dz};
     auto coef_at = [&](int di, int dj, int dk, double &mu, double &lam) {
         const int a = wrapi(i + di, g.m), b = wrapi(j + dj, g.n), c = wrapi(k + dk, g.o);
         const int s = slot(g, a, b, c);
@@ -69,8 +68,7 @@ __device__ void lame_block(const LameOp<double> &op, const Geom &g, int i, int j
         coef_at(0, 0, 0, mu0, lam0);
         coef_at(d[0], d[1], d[2], mu1, lam1);
         const double mu_f = 0.5 * (mu0 + mu1), lam_f = 0.5 * (lam0 + lam1);
-        const double h2 = hh[ax] * hh[ax];
-        for (int c = 0; c < 3; c++) blk[4 * c] = -op.dt * ((c == ax ? (lam_f + 2.0 * mu_f) : mu_f) / h2);
+        for (int c = 0; c < 3; c++) blk[4 * c] = -op.dt * ((c == ax ? (lam_f + 2.0 * mu_f) : mu_f) * op.ih2[ax]);
     } else if (nz == 2) {
         const int r = d[0] ? 0 : 1, c = d[2] ? 2 : 1;
         const int sr = d[r], sc = d[c];
@@ -80,9 +78,9 @@ __device__ void lame_block(const LameOp<double> &op, const Geom &g, int i, int j
         double mu_r, lam_r, mu_c, lam_c;
         coef_at(er[0], er[1], er[2], mu_r, lam_r);
         coef_at(ec[0], ec[1], ec[2], mu_c, lam_c);
-        const double den = 4.0 * hh[r] * hh[c], sgn = (double)(sr * sc);
-        blk[3 * r + c] = -op.dt * ((sgn * (lam_r + mu_c)) / den);
-        blk[3 * c + r] = -op.dt * ((sgn * (lam_c + mu_r)) / den);
+        const double ie = op.iedge[r + c - 1], sgn = (double)(sr * sc);
+        blk[3 * r + c] = -op.dt * ((sgn * (lam_r + mu_c)) * ie);
+        blk[3 * c + r] = -op.dt * ((sgn * (lam_c + mu_r)) * ie);
     }
 }
 

@@ -980,14 +980,14 @@ int stz_mg_set_coeffs_lame(stz_mg_handle h, const double *mu, const double *lam,
         check_launch();
         h->op64[0] = LevelOp<double>{};
         h->op64[0].kind = OP_LAME;
-        h->op64[0].lop = LameOp<double>{h->mu64, h->lam64, dx, dy, dz, dt};
+        h->op64[0].lop = make_lame_op<double>(h->mu64, h->lam64, dx, dy, dz, dt);
         if (h->d.precision == STZ_MG_MIXED) {
             launch_convert(h->mu64, h->mu32, g.npad, h->st);
             launch_convert(h->lam64, h->lam32, g.npad, h->st);
             check_launch();
             h->op32[0] = LevelOp<float>{};
             h->op32[0].kind = OP_LAME;
-            h->op32[0].lop = LameOp<float>{h->mu32, h->lam32, (float)dx, (float)dy, (float)dz, (float)dt};
+            h->op32[0].lop = make_lame_op<float>(h->mu32, h->lam32, dx, dy, dz, dt);
         }
         h->top_kind = OP_LAME;
         sync(h);

@@ -152,7 +152,22 @@ struct LameOp {
     const T *mu;    // colour-blocked, npad
     const T *lam;
     T dx, dy, dz, dt;
+    // reciprocals, so that rows multiply instead of divide (divisions are
+    // expensive, FP64 ones on this GPU especially): 1/h^2 per axis and
+    // 1/(4 h_r h_c) per axis pair (x,y), (x,z), (y,z)
+    T ih2[3], iedge[3];
 };
+
+template <typename T>
+inline LameOp<T> make_lame_op(const T *mu, const T *lam, double dx, double dy, double dz, double dt) {
+    LameOp<T> o;
+    o.mu = mu;
+    o.lam = lam;
+    o.dx = (T)dx; o.dy = (T)dy; o.dz = (T)dz; o.dt = (T)dt;
+    o.ih2[0] = (T)(1.0 / (dx * dx)); o.ih2[1] = (T)(1.0 / (dy * dy)); o.ih2[2] = (T)(1.0 / (dz * dz));
+    o.iedge[0] = (T)(1.0 / (4.0 * dx * dy)); o.iedge[1] = (T)(1.0 / (4.0 * dx * dz)); o.iedge[2] = (T)(1.0 / (4.0 * dy * dz));
+    return o;
+}
 
 // Dense per-node 27-block coefficients (RAT levels).
 template <typename T>

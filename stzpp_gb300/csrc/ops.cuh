@@ -96,7 +96,6 @@ __device__ inline void lame_faces(const LameOp<T> &op, const Geom &g, const NbrO
     const int ctr_x = t.ox[1], ctr_y = t.oy[1], ctr_z = t.oz[1];
     const int sl[6] = {t.ox[0] + ctr_y + ctr_z, t.ox[2] + ctr_y + ctr_z, ctr_x + t.oy[0] + ctr_z,
                        ctr_x + t.oy[2] + ctr_z, ctr_x + ctr_y + t.oz[0], ctr_x + ctr_y + t.oz[2]};
-    const T h2[3] = {op.dx * op.dx, op.dy * op.dy, op.dz * op.dz};
     T cen[3] = {T(0), T(0), T(0)};
 #pragma unroll
     for (int f = 0; f < 6; f++) {
@@ -107,7 +106,7 @@ __device__ inline void lame_faces(const LameOp<T> &op, const Geom &g, const NbrO
         T lam_f = T(0.5) * (lam0 + lam_nb[f]);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            T v = (c == ax ? (lam_f + T(2) * mu_f) : mu_f) / h2[ax];
+            T v = (c == ax ? (lam_f + T(2) * mu_f) : mu_f) * op.ih2[ax];
             L.face[f][c] = -op.dt * v;
             cen[c] -= v;
         }
@@ -135,11 +134,10 @@ __device__ inline void lame_row(const LameOp<T> &op, const Geom &g, const NbrOff
         for (int c = 0; c < 3; c++) acc[c] -= L.face[f][c] * v[c];
     }
     // edges: component pair (r, c) in the plane of axes (r, c)
-    const T hh[3] = {op.dx, op.dy, op.dz};
 #pragma unroll
     for (int pr = 0; pr < 3; pr++) {
         const int r = pr == 2 ? 1 : 0, c = pr == 0 ? 1 : 2;
-        const T den = T(4) * hh[r] * hh[c];
+        const T ie = op.iedge[pr];
 #pragma unroll
         for (int sr = -1; sr <= 1; sr += 2)
 #pragma unroll
@@ -152,8 +150,8 @@ __device__ inline void lame_row(const LameOp<T> &op, const Geom &g, const NbrOff
                 // neighbour coefficient values: lam/mu at p + sr e_r and p + sc e_c
                 const T lam_r = lam_nb[2 * r + (sr > 0)], mu_r = mu_nb[2 * r + (sr > 0)];
                 const T lam_c = lam_nb[2 * c + (sc > 0)], mu_c = mu_nb[2 * c + (sc > 0)];
-                const T a_rc = -op.dt * ((sgn * (lam_r + mu_c)) / den);
-                const T a_cr = -op.dt * ((sgn * (lam_c + mu_r)) / den);
+                const T a_rc = -op.dt * ((sgn * (lam_r + mu_c)) * ie);
+                const T a_cr = -op.dt * ((sgn * (lam_c + mu_r)) * ie);
                 acc[r] -= a_rc * x[sl + c * npad];
                 acc[c] -= a_cr * x[sl + r * npad];
             }
@@ -173,7 +171,7 @@ __device__ inline void lame_row(const LameOp<T> &op, const Geom &g, const NbrOff
 template <typename T>
 __device__ inline T lame_fix(const LameOp<T> &op, int p) {
     const T mu0 = op.mu[p], lam0 = op.lam[p];
-    return (-op.dt * T(2)) * ((lam0 + T(2) * mu0) / op.dx / op.dx + mu0 / op.dy / op.dy + mu0 / op.dz / op.dz);
+    return (-op.dt * T(2)) * ((lam0 + T(2) * mu0) * op.ih2[0] + mu0 * op.ih2[1] + mu0 * op.ih2[2]);
 }
 
 // ---------------------------------------------------------------- dense

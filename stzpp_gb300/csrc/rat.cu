@@ -65,12 +65,11 @@ __device__ inline void fine_block(const LevelOp<double> &op, const Geom &g, int 
             int d[3] = {dx, dy, dz};
             int r = dz == 0 ? 0 : (dy == 0 ? 0 : 1), c = dz == 0 ? 1 : 2;
             int sr = d[r], sc = d[c];
-            const double hh[3] = {op.lop.dx, op.lop.dy, op.lop.dz};
-            const double den = 4.0 * hh[r] * hh[c], sgn = (double)(sr * sc);
+            const double ie = op.lop.iedge[r + c - 1], sgn = (double)(sr * sc);
             const double lam_r = lam_nb[2 * r + (sr > 0)], mu_r = mu_nb[2 * r + (sr > 0)];
             const double lam_c = lam_nb[2 * c + (sc > 0)], mu_c = mu_nb[2 * c + (sc > 0)];
-            a[3 * r + c] = -op.lop.dt * ((sgn * (lam_r + mu_c)) / den);
-            a[3 * c + r] = -op.lop.dt * ((sgn * (lam_c + mu_r)) / den);
+            a[3 * r + c] = -op.lop.dt * ((sgn * (lam_r + mu_c)) * ie);
+            a[3 * c + r] = -op.lop.dt * ((sgn * (lam_c + mu_r)) * ie);
         }
     } else if (KIND == OP_PLANE) {
         const int k = fs;   // callers pass the plane index for plane operators
