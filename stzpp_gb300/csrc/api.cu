@@ -278,6 +278,8 @@ void set_const_op(stz_mg_handle h, const double *stencil, const double *fix) {
         for (int e = 0; e < 9; e++)
             if (!elastic_entry(b, e) && c.a[b][e] != 0.0) elastic = 0;
     c.elastic = elastic;
+    c.centre_diag = c.a[13][1] == 0.0 && c.a[13][2] == 0.0 && c.a[13][3] == 0.0 && c.a[13][5] == 0.0 &&
+                    c.a[13][6] == 0.0 && c.a[13][7] == 0.0;
     ConstOp<float> f{};
     for (int b = 0; b < 27; b++)
         for (int e = 0; e < 9; e++) f.a[b][e] = (float)c.a[b][e];
@@ -287,6 +289,7 @@ void set_const_op(stz_mg_handle h, const double *stencil, const double *fix) {
         f.inv_fix[e] = (float)c.inv_fix[e];
     }
     f.elastic = elastic;
+    f.centre_diag = c.centre_diag;
     h->op64[0] = LevelOp<double>{};
     h->op64[0].kind = OP_CONST;
     h->op64[0].cop = c;

@@ -144,6 +144,7 @@ struct ConstOp {
     T inv_int[9];
     T inv_fix[9];
     int elastic;
+    int centre_diag;   // the centre block a[13] is diagonal
 };
 
 // Per-node Lame coefficients (variable-mu operator, matrix-free).

@@ -72,6 +72,12 @@ __device__ inline void const_row(const ConstOp<T> &op, const Geom &g, const NbrO
 #pragma unroll
             for (int e = 0; e < 9; e++)
                 if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[b][e % 3];
+        } else if (b == 13 && op.centre_diag) {
+            // a diagonal centre block (the elasticity stencil): only its three
+            // non-zero products are formed
+            acc[0] -= op.a[13][0] * v[13][0];
+            acc[1] -= op.a[13][4] * v[13][1];
+            acc[2] -= op.a[13][8] * v[13][2];
         } else {
             matvec_sub(op.a[b], v[b], acc);
         }
