@@ -46,6 +46,10 @@ WORKLOAD = ("quasi-static projection solve, 256x256x257 nodes (257^3 problem: pe
             "mu=1, lambda=2, dx=1/256, RHS = divergence of N(0,1e-3) cell strain (seed 0), x0 = 0, "
             "to relative residual 1e-10")
 CPU_SAMPLE_DIMS = (64, 64, 65)
+# Cycle of the GPU solves: two sweeps down, three up on every level.  Measured
+# at 256x256x257 on a GB300 (mixed / FP64 ms per solve): V(2,2) 44.2 / 242,
+# V(2,3) 41.8 / 222, V(3,3) 43.5 / 231, V(3,2) 45.1 / 222, V(2,1) 53.9 / 260.
+V_DOWN, V_UP = 2, 3
 
 
 def peaks():
@@ -224,8 +228,8 @@ def run_ours(args, world, rank, local):
         return reduce_max(v, dist, "cuda" if dist is None or dist.get_backend() == "nccl" else "cpu")
 
     # ---------------------------------------------------------- mixed solve
-    mg = sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, max_coarse=args.max_coarse, device=local,
-                      stream=stream.cuda_stream)
+    mg = sg.Multigrid(dims, per, precision="mixed", v_down=V_DOWN, v_up=V_UP, sweep_growth=False,
+                      max_coarse=args.max_coarse, device=local, stream=stream.cuda_stream)
     t0 = time.perf_counter()
     mg.setup_matrices(stencil=stencil, fix=fix)
     torch.cuda.synchronize()
@@ -281,7 +285,7 @@ def run_ours(args, world, rank, local):
         ms, work = mg.time_kernel(kid, lvl, reps=20)
         kern[name] = (ms, work)
     # share of a solve: the fine smoother runs (v_down + v_up) sweeps x 8 colours per V-cycle
-    gs_launches = 4 * 8 * vcyc
+    gs_launches = (V_DOWN + V_UP) * 8 * vcyc
     gs_ms, gs_bytes = kern["gs_colour_l0"]
     achieved = gs_bytes / (gs_ms * 1e-3) / 1e9
     r64_ms, r64_flops = kern["residual_fp64"]
@@ -300,8 +304,8 @@ def run_ours(args, world, rank, local):
     mg.close()
 
     # ------------------------------------------------------ FP64 solve
-    mg64 = sg.Multigrid(dims, per, precision="fp64", sweep_growth=False, max_coarse=args.max_coarse, device=local,
-                        stream=stream.cuda_stream)
+    mg64 = sg.Multigrid(dims, per, precision="fp64", v_down=V_DOWN, v_up=V_UP, sweep_growth=False,
+                        max_coarse=args.max_coarse, device=local, stream=stream.cuda_stream)
     mg64.setup_matrices(stencil=stencil, fix=fix)
     mg64.set_rhs(b_dev)
     steps64 = max(2, args.steps // 2)
@@ -327,7 +331,7 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "dims": list(dims), "precision": "mixed: FP32 V-cycles, FP64 residual/update/bottom",
-                       "cycle": ("V(2,2) on every level, 8-colour block GS, RAT coarse operators (plane-invariant "
+                       "cycle": (f"V({V_DOWN},{V_UP}) on every level, 8-colour block GS, RAT coarse operators (plane-invariant "
                                  f"storage), FP64 direct solve of the coarsest level (<= {args.max_coarse} nodes)"),
                        "replicas": world, "l2": "inputs larger than L2 (fine vectors 404 MB each); no flush needed"},
             "cycles": cycles, "relres": rel, "setup_ms": setup_ms,
