@@ -97,15 +97,28 @@ __global__ void interpolation_kernel(Geom gf, Geom gc, const T *__restrict__ xc,
                     load3(xc, gc.npad, slot(gc, X, Y, Z), v[az][ay][ax]);
                 }
             }
+    // the 8 fine values first (all loads in flight together), then the sums
+    // and the stores: the stores cannot be moved ahead of later loads
+    T f[2][2][2][3];
+    int fp[2][2][2];
 #pragma unroll
-    for (int sz = 0; sz < 2; sz++) {
-        if (!ex[2][sz]) continue;
+    for (int sz = 0; sz < 2; sz++)
 #pragma unroll
-        for (int sy = 0; sy < 2; sy++) {
-            if (!ex[1][sy]) continue;
+        for (int sy = 0; sy < 2; sy++)
 #pragma unroll
             for (int sx = 0; sx < 2; sx++) {
-                if (!ex[0][sx]) continue;
+                const bool here = ex[2][sz] && ex[1][sy] && ex[0][sx];
+                fp[sz][sy][sx] = here ? slot(gf, 2 * ci + sx, 2 * cj + sy, 2 * ck + sz) : -1;
+                if (here) load3(xf, gf.npad, fp[sz][sy][sx], f[sz][sy][sx]);
+            }
+#pragma unroll
+    for (int sz = 0; sz < 2; sz++) {
+#pragma unroll
+        for (int sy = 0; sy < 2; sy++) {
+#pragma unroll
+            for (int sx = 0; sx < 2; sx++) {
+                const int p = fp[sz][sy][sx];
+                if (p < 0) continue;
                 // parents per dimension: s = 0 -> {c}; s = 1 -> {c, c+1} or {c+1} (collapse)
                 const int z0 = (sz && col[2]) ? 1 : 0, z1 = sz && !col[2] ? 1 : z0;
                 const int y0 = (sy && col[1]) ? 1 : 0, y1 = sy && !col[1] ? 1 : y0;
@@ -125,10 +138,9 @@ __global__ void interpolation_kernel(Geom gf, Geom gc, const T *__restrict__ xc,
                             cnt++;
                         }
                 const T w = T(1) / T(cnt);
-                const int p = slot(gf, 2 * ci + sx, 2 * cj + sy, 2 * ck + sz);
-                xf[p] += w * s3[0];
-                xf[p + gf.npad] += w * s3[1];
-                xf[p + 2 * gf.npad] += w * s3[2];
+                xf[p] = f[sz][sy][sx][0] + w * s3[0];
+                xf[p + gf.npad] = f[sz][sy][sx][1] + w * s3[1];
+                xf[p + 2 * gf.npad] = f[sz][sy][sx][2] + w * s3[2];
             }
         }
     }
