@@ -133,9 +133,9 @@ __global__ void adjoint_dirichlet_kernel(Geom g, const __grid_constant__ ConstOp
                 }
         if (KIND == OP_CONST) {
             const double *f = cop.inv_fix;   // w_D = F^{-T} acc
-            w[3 * q] = f[0] * acc[0] + f[3] * acc[1] + f[6] * acc[2];
-            w[3 * q + 1] = f[1] * acc[0] + f[4] * acc[1] + f[7] * acc[2];
-            w[3 * q + 2] = f[2] * acc[0] + f[5] * acc[1] + f[8] * acc[2];
+            w[3 * q] = dot3(f[0], acc[0], f[3], acc[1], f[6], acc[2]);
+            w[3 * q + 1] = dot3(f[1], acc[0], f[4], acc[1], f[7], acc[2]);
+            w[3 * q + 2] = dot3(f[2], acc[0], f[5], acc[1], f[8], acc[2]);
         } else {
             const int s = slot(g, i, j, k);
             const double f = lame_fix(lop, s);
@@ -206,7 +206,7 @@ __global__ void lame_grad_rows_kernel(Geom g, LameOp<double> op, const double *_
             }
         } else {
             // Dirichlet row: fix(mu, lam) u_p, fix = -2 dt ((lam + 2 mu)/dx^2 + mu/dy^2 + mu/dz^2)
-            const double wu = wp[0] * up[0] + wp[1] * up[1] + wp[2] * up[2];
+            const double wu = dot3(wp[0], up[0], wp[1], up[1], wp[2], up[2]);
             const double ix2 = 1.0 / (op.dx * op.dx), iy2 = 1.0 / (op.dy * op.dy), iz2 = 1.0 / (op.dz * op.dz);
             gm[0] = 2.0 * op.dt * (2.0 * ix2 + iy2 + iz2) * wu;
             gl[0] = 2.0 * op.dt * ix2 * wu;

@@ -190,11 +190,26 @@ struct PlaneOp {
     int sparse;
 };
 
+// Round-to-nearest product and fused multiply-add, overloaded on the type.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// a0 b0 + a1 b1 + a2 b2, always rounded as fma(a2, b2, fma(a1, b1, a0 b0)):
+// written as a plain expression the compiler may fuse either product, and
+// kernels that must agree bit for bit (the tiled and the colour sweeps and
+// residuals) could then round differently.
+template <typename T>
+__device__ __forceinline__ T dot3(T a0, T b0, T a1, T b1, T a2, T b2) {
+    return fma_rn(a2, b2, fma_rn(a1, b1, mul_rn(a0, b0)));
+}
+
 template <typename T>
 __device__ inline void matvec_sub(const T *a, const T *v, T *acc) {
-    acc[0] -= a[0] * v[0] + a[1] * v[1] + a[2] * v[2];
-    acc[1] -= a[3] * v[0] + a[4] * v[1] + a[5] * v[2];
-    acc[2] -= a[6] * v[0] + a[7] * v[1] + a[8] * v[2];
+    acc[0] -= dot3(a[0], v[0], a[1], v[1], a[2], v[2]);
+    acc[1] -= dot3(a[3], v[0], a[4], v[1], a[5], v[2]);
+    acc[2] -= dot3(a[6], v[0], a[7], v[1], a[8], v[2]);
 }
 
 template <typename T>

@@ -34,6 +34,15 @@ template <typename T>
 bool gs_tile_applies(const LevelOp<T> &op, const Geom &g);
 template <typename T>
 void launch_gs_sweep_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st);
+// tile.cu: res = r - A x by plane tiles staged in shared memory; with
+// partial non-null, per-CTA sums of |res|^2
+template <typename T>
+bool residual_tile_applies(const LevelOp<T> &op, const Geom &g);
+// the tiled residual's CTA count (its number of norm partials)
+int residual_tile_blocks(const Geom &g);
+template <typename T>
+void launch_residual_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, double *partial,
+                          cudaStream_t st);
 int residual_blocks(const Geom &g);
 // res = r - A x (res may be null); when partial is non-null, per-block sums of
 // |res|^2 go to partial[residual_blocks(g)] and, when out is non-null, their

@@ -12,6 +12,7 @@
 // is deterministic.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 
 #include "launch.h"
 #include "ops.cuh"
@@ -46,9 +47,9 @@ __global__ void __launch_bounds__(kBlock) gs_const_kernel(Geom g, int q, int k0,
     } else {
         inv = op.inv_fix;
     }
-    x[p] = inv[0] * acc[0] + inv[1] * acc[1] + inv[2] * acc[2];
-    x[p + g.npad] = inv[3] * acc[0] + inv[4] * acc[1] + inv[5] * acc[2];
-    x[p + 2 * g.npad] = inv[6] * acc[0] + inv[7] * acc[1] + inv[8] * acc[2];
+    x[p] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+    x[p + g.npad] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+    x[p + 2 * g.npad] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
 }
 
 template <typename T>
@@ -84,9 +85,9 @@ __global__ void __launch_bounds__(kBlock) gs_dense_kernel(Geom g, int q, int k0,
     T inv[9];
 #pragma unroll
     for (int e = 0; e < 9; e++) inv[e] = __ldg(op.dinv + (size_t)e * np + p);
-    x[p] = inv[0] * acc[0] + inv[1] * acc[1] + inv[2] * acc[2];
-    x[p + g.npad] = inv[3] * acc[0] + inv[4] * acc[1] + inv[5] * acc[2];
-    x[p + 2 * g.npad] = inv[6] * acc[0] + inv[7] * acc[1] + inv[8] * acc[2];
+    x[p] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+    x[p + g.npad] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+    x[p + 2 * g.npad] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
 }
 
 // Plane-invariant levels: every block of the 3-D grid lies on one sub-grid
@@ -108,9 +109,9 @@ __global__ void __launch_bounds__(kBlock) gs_plane_kernel(Geom g, int q, int k0,
     NbrOffsets nb = nbr_offsets_sub(g, I, J, K, q & 1, (q >> 1) & 1, q >> 2);
     plane_row_coef<T, SPARSE, false>(cf, 1, g, nb, x, acc);
     const T *inv = cf + 243;
-    x[p] = inv[0] * acc[0] + inv[1] * acc[1] + inv[2] * acc[2];
-    x[p + g.npad] = inv[3] * acc[0] + inv[4] * acc[1] + inv[5] * acc[2];
-    x[p + 2 * g.npad] = inv[6] * acc[0] + inv[7] * acc[1] + inv[8] * acc[2];
+    x[p] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+    x[p + g.npad] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+    x[p + 2 * g.npad] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
 }
 
 // ------------------------------------------------------ plane-phase sweep
@@ -161,9 +162,9 @@ __device__ inline void gs_node(const LevelOp<T> &op, const Geom &g, int q, int I
 #pragma unroll
         for (int e = 0; e < 9; e++) inv[e] = __ldg(op.dop.dinv + (size_t)e * np + p);
     }
-    x[p] = inv[0] * acc[0] + inv[1] * acc[1] + inv[2] * acc[2];
-    x[p + g.npad] = inv[3] * acc[0] + inv[4] * acc[1] + inv[5] * acc[2];
-    x[p + 2 * g.npad] = inv[6] * acc[0] + inv[7] * acc[1] + inv[8] * acc[2];
+    x[p] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+    x[p + g.npad] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+    x[p + 2 * g.npad] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
 }
 
 constexpr int kPhaseThreads = 512;
@@ -388,6 +389,11 @@ static void launch_residual_k(const LevelOp<T> &op, const Geom &g, const T *r, c
 template <typename T, typename R>
 void launch_residual(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, R *res, double *partial,
                      double *out, cudaStream_t st) {
+    if (std::is_same<T, R>::value && res && residual_tile_applies(op, g)) {
+        launch_residual_tile<T>(op, g, r, x, reinterpret_cast<T *>(res), partial, st);
+        if (partial && out) sum_partials_kernel<<<1, 1024, 0, st>>>(partial, residual_tile_blocks(g), out);
+        return;
+    }
     if (partial) launch_residual_k<T, R, true>(op, g, r, x, res, partial, st);
     else launch_residual_k<T, R, false>(op, g, r, x, res, partial, st);
     if (partial && out) sum_partials_kernel<<<1, 1024, 0, st>>>(partial, residual_blocks(g), out);

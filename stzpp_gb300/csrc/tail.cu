@@ -55,9 +55,9 @@ __device__ inline void tail_gs_node(const TailLev<T> &L, int q, int t, const T *
 #pragma unroll
         for (int e = 0; e < 9; e++) inv[e] = __ldg(L.dinv + (size_t)e * g.npad + p);
     }
-    L.x[p] = inv[0] * acc[0] + inv[1] * acc[1] + inv[2] * acc[2];
-    L.x[p + g.npad] = inv[3] * acc[0] + inv[4] * acc[1] + inv[5] * acc[2];
-    L.x[p + 2 * g.npad] = inv[6] * acc[0] + inv[7] * acc[1] + inv[8] * acc[2];
+    L.x[p] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+    L.x[p + g.npad] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+    L.x[p + 2 * g.npad] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
 }
 
 template <typename T>

@@ -224,21 +224,58 @@ def test_tiled_sweep_is_the_colour_sweep(dims, per, level, sweeps, monkeypatch):
     assert np.array_equal(out["0"], out["1"])
 
 
-def test_tiled_sweep_mixed_solve_bitwise(monkeypatch):
-    """The FP32 V-cycles of the mixed solve with and without the tiled sweep
-    give the same cycle count and the same solution bit for bit."""
+RES_TILE_CASES = [((64, 64, 17), (True, True, False), "const", 0), ((64, 64, 16), (True, True, True), "const", 0),
+                  ((64, 64, 17), (True, True, False), "trans", 0), ((96, 64, 8), (True, True, True), "trans", 0),
+                  ((128, 128, 17), (True, True, False), "const", 1), ((128, 128, 16), (True, True, True), "trans", 1)]
+
+
+@pytest.mark.parametrize("dims,per,kind,level", RES_TILE_CASES)
+def test_tiled_residual_is_the_colour_residual(dims, per, kind, level, monkeypatch):
+    """The tiled residual (a CTA per plane tile, neighbours from shared
+    memory) gives bit-for-bit the residual of the colour-interleaved kernel,
+    and the same |res|^2 up to summation order: FP64 level residuals of the
+    elastic and of a full non-symmetric shared stencil and of their
+    plane-invariant coarse operators, Dirichlet and periodic z."""
     import stzpp_gb300 as sg
-    dims, per = (128, 128, 33), (True, True, False)
     m, n, o = dims
-    h = P.grid_spacing(m, n, o, per, h=1.0 / 128)   # isotropic: the cycle converges
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz) if kind == "const" else trans_stencil(2, dx)
+    out = {}
+    for tile in ("0", "1"):   # 1: the tiled residual also in FP64
+        monkeypatch.setenv("STZ_MG_TILE", tile)
+        with sg.Multigrid(dims, per, precision="fp64", bottom="gs", max_coarse=5000) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            N = mg.level_npts(level)
+            rng = np.random.default_rng(9)
+            mg.level_set_field(level, "x", rng.standard_normal((N, 3)))
+            mg.level_set_field(level, "r", rng.standard_normal((N, 3)))
+            out[tile] = mg.residual(level)
+    assert np.array_equal(out["0"][0], out["1"][0])
+    assert abs(out["0"][1] - out["1"][1]) <= 1e-12 * out["0"][1]
+
+
+@pytest.mark.parametrize("dims,per,kind", [((128, 128, 33), (True, True, False), "const"),
+                                             ((128, 128, 33), (True, True, False), "trans")])
+def test_tiled_sweep_mixed_solve_bitwise(dims, per, kind, monkeypatch):
+    """The FP32 V-cycles of the mixed solve with and without the tiled kernels
+    (the tiled sweep and the tiled FP32 residual) give the same cycle count
+    and the same solution bit for bit: the elastic and a full non-symmetric
+    shared stencil, Dirichlet and periodic z."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per, h=1.0 / m)   # isotropic: the cycle converges
     b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
     out = {}
-    for tile in ("0", "1"):   # 1: the tiled sweep on every level it applies to
+    for tile in ("0", "1"):   # 1: the tiled kernels on every level they apply to
         monkeypatch.setenv("STZ_MG_TILE", tile)
         with sg.Multigrid(dims, per, precision="mixed", sweep_growth=False) as mg:
-            mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, *h))
+            if kind == "const":
+                mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, *h))
+            else:
+                mg.setup_matrices(*trans_stencil(2, h[0]))
             mg.setup_fields(r=b)
-            cyc, rel = mg.solve(1e-10, 100)
-            out[tile] = (cyc, mg.get_x())
-    assert out["0"][0] == out["1"][0]
-    assert np.array_equal(out["0"][1], out["1"][1])
+            cyc, rel = mg.solve(1e-10, 6, check=False)
+            out[tile] = (cyc, rel, mg.get_x())
+    assert np.isfinite(out["0"][1]) and out["0"][1] < 1e-3
+    assert out["0"][:2] == out["1"][:2]
+    assert np.array_equal(out["0"][2], out["1"][2])
