@@ -39,7 +39,7 @@ void launch_gs_sweep_tile(const LevelOp<T> &op, const Geom &g, const T *r, const
 template <typename T>
 bool residual_tile_applies(const LevelOp<T> &op, const Geom &g);
 // the tiled residual's CTA count (its number of norm partials)
-int residual_tile_blocks(const Geom &g);
+int residual_tile_blocks(const Geom &g, bool fp64);
 template <typename T>
 void launch_residual_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, double *partial,
                           cudaStream_t st);

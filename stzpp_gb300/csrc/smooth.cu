@@ -391,7 +391,7 @@ void launch_residual(const LevelOp<T> &op, const Geom &g, const T *r, const T *x
                      double *out, cudaStream_t st) {
     if (std::is_same<T, R>::value && res && residual_tile_applies(op, g)) {
         launch_residual_tile<T>(op, g, r, x, reinterpret_cast<T *>(res), partial, st);
-        if (partial && out) sum_partials_kernel<<<1, 1024, 0, st>>>(partial, residual_tile_blocks(g), out);
+        if (partial && out) sum_partials_kernel<<<1, 1024, 0, st>>>(partial, residual_tile_blocks(g, sizeof(T) == 8), out);
         return;
     }
     if (partial) launch_residual_k<T, R, true>(op, g, r, x, res, partial, st);

@@ -26,6 +26,7 @@
 // is bit-identical to the eight colour launches.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 
 #include "launch.h"
 #include "ops.cuh"
@@ -35,11 +36,20 @@ namespace stzmg {
 namespace {
 
 constexpr int kTX = 32, kTY = 32, kHalo = 4;
-constexpr int kSX = kTX + 2 * kHalo, kSY = kTY + 2 * kHalo;
+constexpr int kSY = kTY + 2 * kHalo;
 // Each half-row (one x-parity) is staged as the 16-byte-aligned window of
 // kHW sub-grid slots starting 4 slots before the tile (the halo needs 2).
 constexpr int kHW = kTX / 2 + 8, kHOff = 2;
 constexpr int kTileThreads = 256;
+// CTAs per SM the shared memory allows (3 in FP32, 1 in FP64): lets ptxas
+// give each thread the registers those CTAs leave, for more loads in flight.
+template <typename T>
+constexpr int kTileMinBlocks = sizeof(T) == 4 ? 3 : 1;
+// Threads of the tiled sweep: every phase (at most 19 x 19 nodes) in one round.
+constexpr int kGsThreads = 384;
+constexpr int RS = 2 * kHW;   // words per row of one component plane
+constexpr int CS = kSY * RS;  // words per component plane
+constexpr int PS = 3 * CS;    // words per buffer plane
 
 __device__ __forceinline__ int wrapn(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
@@ -51,11 +61,59 @@ struct TileBuf {
     T v[3][3][kSY][2][kHW];
 };
 
+// Rows of one buffer component plane: the sweep stages rows 0 .. kSY - 1 of
+// the widened tile, the residual rows kHalo - 1 .. kHalo + kTY (one beyond
+// the tile) into buffer rows 0 .. kRowsRes - 1.
+constexpr int kRowsRes = kTY + 2, kRes0 = kHalo - 1;
+
+// A node's neighbours in one buffer plane are read relative to its "corner"
+// word there: row jj - 1, slot (ii >> 1) + kHOff - 1 of the x-parity-0
+// half-row.  Neighbour (bdx, bdy)(b), component c, of a node of x-parity A is
+// then at this non-negative compile-time word offset, in a buffer plane of
+// NROWS rows per component (the node itself: b = 13, in its own plane).
+template <int A, int NROWS>
+__host__ __device__ constexpr int nb_off(int b, int c) {
+    return c * NROWS * RS + (bdy(b) + 1) * RS + ((A + bdx(b) + 2) & 1) * kHW + ((A + bdx(b) + 2) >> 1);
+}
+
+// Corner word of node (ii, jj) in a buffer plane whose row 0 is tile row ROW0.
+template <int ROW0>
+__device__ __forceinline__ int corner_word(int ii, int jj) {
+    return (jj - 1 - ROW0) * RS + (ii >> 1) + kHOff - 1;
+}
+
+// Shared-memory load / store at a compile-time byte offset from a 32-bit
+// shared address: one instruction per access, no per-access address arithmetic.
+template <int OFF>
+__device__ __forceinline__ void lds(unsigned a, float &v) {
+    asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(a), "n"(OFF * 4));
+}
+template <int OFF>
+__device__ __forceinline__ void lds(unsigned a, double &v) {
+    asm volatile("ld.shared.f64 %0, [%1+%2];" : "=d"(v) : "r"(a), "n"(OFF * 8));
+}
+template <int OFF>
+__device__ __forceinline__ void sts(unsigned a, float v) {
+    asm volatile("st.shared.f32 [%0+%1], %2;" ::"r"(a), "n"(OFF * 4), "f"(v) : "memory");
+}
+template <int OFF>
+__device__ __forceinline__ void sts(unsigned a, double v) {
+    asm volatile("st.shared.f64 [%0+%1], %2;" ::"r"(a), "n"(OFF * 8), "d"(v) : "memory");
+}
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I = B .. E - 1.
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
 // Asynchronous 16-byte global -> shared copy (cp.async, no register round
 // trip): every copy of a tile is in flight at once.  Both addresses are
-// 16-byte aligned (sub-grid rows and slot windows are multiples of 4 floats).
-__device__ __forceinline__ void copy16_async(void *dst, const void *src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+// 16-byte aligned (sub-grid rows and slot windows are multiples of 16 bytes).
+__device__ __forceinline__ void copy16_async(unsigned d, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 
@@ -64,102 +122,159 @@ __device__ __forceinline__ void copy_wait() {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-// Issue the copies of plane k of the widened tile (rows j0 + JLO .. j0 + JLO
-// + NR - 1, slot window starting at sub-grid column w0, periodic) from x into
-// buffer plane pl, in 16-byte chunks; completed by copy_wait().
-template <typename T, int JLO = 0, int NR = kSY>
-__device__ void stage_plane(const Geom &g, const T *__restrict__ x, int k, int w0, int j0, TileBuf<T> &B, int pl) {
-    constexpr int E = 16 / sizeof(T), NC = kHW / E;   // elements per chunk, chunks per half-row
-    const size_t np = (size_t)g.npad;
-    const int kq = (k & 1) << 2, kofs = (k >> 1) * g.N2;
-    for (int idx = threadIdx.x; idx < 3 * NR * 2 * NC; idx += kTileThreads) {
-        const int cn = idx % NC, r1 = idx / NC;        // chunk fastest: consecutive sub-grid slots
-        const int p = r1 & 1, r2 = r1 >> 1;
-        const int jj = JLO + r2 % NR, cc = r2 / NR;
-        const int j = wrapn(j0 + jj, g.n);
-        const int I = wrapn(w0 + cn * E, g.M2);        // a chunk never straddles the wrap (M2 % E == 0)
-        const size_t s = (size_t)(kq + ((j & 1) << 1) + p) * g.S + (size_t)(kofs + (j >> 1)) * g.M2 + I + cc * np;
-        copy16_async(&B.v[pl][cc][jj][p][cn * E], x + s);
+// The 16-byte copies that stage one plane of the widened tile (rows JLO ..
+// JLO + NR - 1, the kHW-slot window from sub-grid column w0 of each half-row,
+// periodic in x and y) into a buffer plane of NROWS rows per component whose
+// row 0 is tile row ROW0.  Each thread works out its share once per CTA: the
+// chunk's place in a buffer component plane and its offset inside a plane of
+// one colour sub-grid, which is the same for every plane and component.
+template <typename T, int JLO, int NR, int ROW0, int NROWS, int NT = kTileThreads>
+struct Stager {
+    static constexpr int E = 16 / sizeof(T), NC = kHW / E, NCH = NR * 2 * NC;
+    static constexpr int ND = (NCH + NT - 1) / NT;
+    unsigned soff[ND];   // bytes from the start of a buffer component plane
+    int goff[ND];        // elements from the plane's start in colour sub-grid 0 (-1: none)
+
+    __device__ __forceinline__ void init(const Geom &g, int w0, int j0) {
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            const int idx = (int)threadIdx.x + d * NT;
+            goff[d] = -1;
+            soff[d] = 0;
+            if (idx < NCH) {
+                const int cn = idx % NC, r1 = idx / NC;   // chunk fastest: consecutive sub-grid slots
+                const int p = r1 & 1, jj = JLO + (r1 >> 1);
+                const int j = wrapn(j0 + jj, g.n);
+                const int I = wrapn(w0 + cn * E, g.M2);    // a chunk never straddles the wrap (M2 % E == 0)
+                goff[d] = (((j & 1) << 1) + p) * g.S + (j >> 1) * g.M2 + I;
+                soff[d] = (unsigned)((((jj - ROW0) * 2 + p) * kHW + cn * E) * (int)sizeof(T));
+            }
+        }
+    }
+
+    // Issue the copies of plane k of x into the buffer plane at shared byte
+    // address dk; completed by a cp.async wait.
+    __device__ __forceinline__ void stage(const Geom &g, const T *__restrict__ x, int k, unsigned dk) const {
+        const T *xk = x + (size_t)((k & 1) << 2) * g.S + (size_t)(k >> 1) * g.N2 * g.M2;
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            const T *xc = xk + (size_t)cc * g.npad;
+            const unsigned dc = dk + (unsigned)(cc * NROWS * RS * (int)sizeof(T));
+#pragma unroll
+            for (int d = 0; d < ND; d++)
+                if (goff[d] >= 0) copy16_async(dc + soff[d], xc + goff[d]);
+        }
+    }
+};
+
+// acc -= sum_b A_b x_b of the shared stencil in the order and arithmetic of
+// const_row (ops.cuh): neighbour components first (those the stencil uses),
+// then the products.  WITH_CENTRE: include the centre block (residual).
+template <typename T, bool ELASTIC, bool WITH_CENTRE, int A, int NROWS>
+__device__ __forceinline__ void tile_const_row(const ConstOp<T> &op, const unsigned (&cz)[3], T *acc) {
+    T v[27][3];
+    static_for<0, 27>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        if constexpr ((b != 13 || WITH_CENTRE) && !(ELASTIC && nnz_axes(b) == 3)) {
+            static_for<0, 3>([&](auto ci) {
+                constexpr int c = decltype(ci)::value;
+                constexpr bool used = !ELASTIC || b == 13 || elastic_entry(b, c) || elastic_entry(b, 3 + c) ||
+                                      elastic_entry(b, 6 + c);
+                if constexpr (used) lds<nb_off<A, NROWS>(b, c)>(cz[bdz(b) + 1], v[b][c]);
+                else v[b][c] = T(0);
+            });
+        }
+    });
+#pragma unroll
+    for (int b = 0; b < 27; b++) {
+        if (b == 13 && !WITH_CENTRE) continue;
+        if (ELASTIC && nnz_axes(b) == 3) continue;
+        if (ELASTIC && b != 13) {
+#pragma unroll
+            for (int e = 0; e < 9; e++)
+                if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[b][e % 3];
+        } else if (b == 13 && op.centre_diag) {
+            acc[0] -= op.a[13][0] * v[13][0];
+            acc[1] -= op.a[13][4] * v[13][1];
+            acc[2] -= op.a[13][8] * v[13][2];
+        } else {
+            matvec_sub(op.a[b], v[b], acc);
+        }
     }
 }
 
-// Phase N (colour (a, b) = (N & 1, N >> 1) of the plane): every node of that
-// colour in the tile widened by 3 - N.  All parities and widths are
+// acc -= sum_b A_b x_b with block b's entries in cf[9b ..] (shared memory):
+// the order and arithmetic of plane_row_coef (ops.cuh); a neighbour beyond a
+// Dirichlet z-boundary contributes nothing.  One block at a time: hoisting
+// all 243 coefficient and 78 neighbour reads into registers would cost
+// occupancy.
+template <typename T, bool SPARSE, bool WITH_CENTRE, int A, int NROWS>
+__device__ __forceinline__ void tile_plane_row(const T *cf, const unsigned (&cz)[3], bool has_lo, bool has_hi,
+                                               T *acc) {
+    static_for<0, 27>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        if constexpr (b != 13 || WITH_CENTRE) {
+            asm volatile("" ::: "memory");
+            const bool out = (bdz(b) < 0 && !has_lo) || (bdz(b) > 0 && !has_hi);
+            T vv[3];
+            lds<nb_off<A, NROWS>(b, 0)>(cz[bdz(b) + 1], vv[0]);
+            lds<nb_off<A, NROWS>(b, 1)>(cz[bdz(b) + 1], vv[1]);
+            lds<nb_off<A, NROWS>(b, 2)>(cz[bdz(b) + 1], vv[2]);
+            if (out) vv[0] = vv[1] = vv[2] = T(0);
+#pragma unroll
+            for (int e = 0; e < 9; e++)
+                if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[9 * b + e] * vv[e % 3];
+        }
+    });
+}
+
+// Phase N updates colour (a, b) = (N & 1, N >> 1) of the plane on the tile
+// widened by 3 - N: nx x ny nodes, at most one per thread.  This thread's
+// node (if any): its tile coordinates (ii, jj) and sub-grid slot s.
+template <int N>
+struct Phase {
+    static constexpr int a = N & 1, b = N >> 1, ext = 3 - N;
+    static constexpr int lox = kHalo - ext + ((kHalo - ext + a) & 1), loy = kHalo - ext + ((kHalo - ext + b) & 1);
+    static constexpr int nx = (kHalo + kTX + ext - lox + 1) / 2, ny = (kHalo + kTY + ext - loy + 1) / 2;
+    static_assert(nx * ny <= kGsThreads, "one node per thread");
+
+    __device__ __forceinline__ static bool node(const Geom &g, int c, int k, int i0, int j0, int &ii, int &jj,
+                                                int &s) {
+        const int t = (int)threadIdx.x;
+        if (t >= nx * ny) return false;
+        const int yy = t / nx, xx = t - yy * nx;
+        ii = lox + 2 * xx;
+        jj = loy + 2 * yy;
+        const int i = wrapn(i0 + ii, g.m), j = wrapn(j0 + jj, g.n);
+        s = (N + 4 * c) * g.S + ((k >> 1) * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
+        return true;
+    }
+};
+
+// Phase N: every node of its colour in the widened tile, with r of this
+// thread's nodes already in registers (rr).  All parities and widths are
 // compile-time, so a neighbour read is one shared load at a fixed offset from
-// the node's own address.
+// the node's corner address.
 template <typename T, int KIND, bool ELASTIC, bool SPARSE, int N>
 __device__ __forceinline__ void tile_phase(const Geom &g, int c, int k, int i0, int j0, bool zin, bool has_lo,
-                                           bool has_hi, const LevelOp<T> &op, const T *cf, TileBuf<T> &B,
-                                           const T *__restrict__ r, T *__restrict__ xout) {
-    constexpr int a = N & 1, b = N >> 1, ext = 3 - N;
-    constexpr int lox = kHalo - ext + ((kHalo - ext + a) & 1), loy = kHalo - ext + ((kHalo - ext + b) & 1);
-    constexpr int nx = (kHalo + kTX + ext - lox + 1) / 2, ny = (kHalo + kTY + ext - loy + 1) / 2;
-    constexpr int RS = 2 * kHW;                  // words per row of one component plane
-    constexpr int CS = kSY * RS;                 // words per component plane
+                                           bool has_hi, const LevelOp<T> &op, const T *cf, unsigned sbase,
+                                           const T (&rr)[3], T *__restrict__ xout) {
+    constexpr int a = Phase<N>::a;
     const size_t np = (size_t)g.npad;
-    const int q = N + 4 * c, K = k >> 1;
-    T *const flat = &B.v[0][0][0][0][0];
-    for (int t = threadIdx.x; t < nx * ny; t += kTileThreads) {
-        const int yy = t / nx, xx = t - yy * nx;
-        const int ii = lox + 2 * xx, jj = loy + 2 * yy;
-        const int i = wrapn(i0 + ii, g.m), j = wrapn(j0 + jj, g.n);
-        const int s = q * g.S + (K * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
-        T acc[3] = {r[s], r[s + np], r[s + 2 * np]};
-        // plane k is the middle buffer plane: component cc of it starts at (3 + cc) * CS
-        T *const self = flat + 3 * CS + jj * RS + a * kHW + (ii >> 1) + kHOff;
-        // neighbour (bdx, bdy, bdz)(bb), component cc
-        auto fetch = [&](int bb, int cc) -> T {
-            const int dx = bdx(bb), dy = bdy(bb), dz = bdz(bb);
-            return self[(dz * 3 + cc) * CS + dy * RS + (((a + dx) & 1) - a) * kHW + ((a + dx) >> 1)];
-        };
+    int ii, jj, s;
+    if (Phase<N>::node(g, c, k, i0, j0, ii, jj, s)) {
+        T acc[3] = {rr[0], rr[1], rr[2]};
+        constexpr unsigned PB = 3 * kSY * RS * sizeof(T);   // bytes per buffer plane
+        const unsigned c1 = sbase + (unsigned)(corner_word<0>(ii, jj) * (int)sizeof(T));
+        const unsigned cz[3] = {c1, c1 + PB, c1 + 2 * PB};
         T inv[9];
         if (KIND == OP_PLANE || zin) {
             if (KIND == OP_CONST) {
-                // the order and arithmetic of const_row (ops.cuh)
-                T v[27][3];
-#pragma unroll
-                for (int bb = 0; bb < 27; bb++) {
-                    if (bb == 13) continue;
-                    if (ELASTIC && nnz_axes(bb) == 3) continue;
-#pragma unroll
-                    for (int cc = 0; cc < 3; cc++) {
-                        bool used = !ELASTIC;
-#pragma unroll
-                        for (int rr = 0; rr < 3; rr++) used = used || elastic_entry(bb, 3 * rr + cc);
-                        v[bb][cc] = used ? fetch(bb, cc) : T(0);
-                    }
-                }
-#pragma unroll
-                for (int bb = 0; bb < 27; bb++) {
-                    if (bb == 13) continue;
-                    if (ELASTIC && nnz_axes(bb) == 3) continue;
-                    if (ELASTIC) {
-#pragma unroll
-                        for (int e = 0; e < 9; e++)
-                            if (elastic_entry(bb, e)) acc[e / 3] -= op.cop.a[bb][e] * v[bb][e % 3];
-                    } else {
-                        matvec_sub(op.cop.a[bb], v[bb], acc);
-                    }
-                }
+                tile_const_row<T, ELASTIC, false, a, kSY>(op.cop, cz, acc);
 #pragma unroll
                 for (int e = 0; e < 9; e++) inv[e] = op.cop.inv_int[e];
             } else {
-                // the order and arithmetic of plane_row_coef (ops.cuh); a
-                // neighbour beyond a Dirichlet z-boundary contributes nothing
-#pragma unroll
-                for (int bb = 0; bb < 27; bb++) {
-                    if (bb == 13) continue;
-                    // one block at a time: hoisting all 243 coefficient and
-                    // 78 neighbour reads into registers would cost occupancy
-                    asm volatile("" ::: "memory");
-                    const bool out = (bdz(bb) < 0 && !has_lo) || (bdz(bb) > 0 && !has_hi);
-                    T vv[3];
-#pragma unroll
-                    for (int cc = 0; cc < 3; cc++) vv[cc] = out ? T(0) : fetch(bb, cc);
-#pragma unroll
-                    for (int e = 0; e < 9; e++)
-                        if (!SPARSE || coarse_entry(bb, e)) acc[e / 3] -= cf[9 * bb + e] * vv[e % 3];
-                }
+                tile_plane_row<T, SPARSE, false, a, kSY>(cf, cz, has_lo, has_hi, acc);
 #pragma unroll
                 for (int e = 0; e < 9; e++) inv[e] = cf[243 + e];
             }
@@ -170,9 +285,9 @@ __device__ __forceinline__ void tile_phase(const Geom &g, int c, int k, int i0, 
         const T n0 = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
         const T n1 = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
         const T n2 = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
-        self[0] = n0;
-        self[CS] = n1;
-        self[2 * CS] = n2;
+        sts<nb_off<a, kSY>(13, 0)>(cz[1], n0);
+        sts<nb_off<a, kSY>(13, 1)>(cz[1], n1);
+        sts<nb_off<a, kSY>(13, 2)>(cz[1], n2);
         if (ii >= kHalo && ii < kHalo + kTX && jj >= kHalo && jj < kHalo + kTY) {
             xout[s] = n0;
             xout[s + np] = n1;
@@ -182,11 +297,11 @@ __device__ __forceinline__ void tile_phase(const Geom &g, int c, int k, int i0, 
 }
 
 template <typename T, int KIND, bool ELASTIC, bool SPARSE>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kGsThreads, kTileMinBlocks<T>)
     gs_tile_kernel(Geom g, int c, const __grid_constant__ LevelOp<T> op, const T *__restrict__ r,
                    const T *__restrict__ xin, T *__restrict__ xout) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileBuf<T> &B = *reinterpret_cast<TileBuf<T> *>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     __shared__ T cf[KIND == OP_PLANE ? 252 : 1];
     const int ntx = g.m / kTX;
     const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
@@ -198,127 +313,179 @@ __global__ void __launch_bounds__(kTileThreads)
     const bool zin = g.zp || (k != 0 && k != g.o - 1);
 
     if (KIND == OP_PLANE)
-        for (int e = threadIdx.x; e < 252; e += kTileThreads)
+        for (int e = threadIdx.x; e < 252; e += kGsThreads)
             cf[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
-    const int w0 = (i0 >> 1) - kHOff;   // first staged sub-grid column, a multiple of 4
-    stage_plane(g, xin, k, w0, j0, B, 1);
-    if (has_lo) stage_plane(g, xz, k == 0 ? g.o - 1 : k - 1, w0, j0, B, 0);
-    if (has_hi) stage_plane(g, xz, k == g.o - 1 ? 0 : k + 1, w0, j0, B, 2);
+    constexpr unsigned PB = 3 * kSY * RS * sizeof(T);   // bytes per buffer plane
+    Stager<T, 0, kSY, 0, kSY, kGsThreads> st;
+    st.init(g, (i0 >> 1) - kHOff, j0);   // first staged sub-grid column: a multiple of 4
+    st.stage(g, xin, k, sbase + PB);
+    if (has_lo) st.stage(g, xz, k == 0 ? g.o - 1 : k - 1, sbase);
+    if (has_hi) st.stage(g, xz, k == g.o - 1 ? 0 : k + 1, sbase + 2 * PB);
+    // r of every node this thread updates, loaded while the copies are in flight
+    const size_t np = (size_t)g.npad;
+    T rr[4][3];
+    static_for<0, 4>([&](auto ni) {
+        constexpr int N = decltype(ni)::value;
+        int ii, jj, s;
+        if (Phase<N>::node(g, c, k, i0, j0, ii, jj, s)) {
+            rr[N][0] = r[s];
+            rr[N][1] = r[s + np];
+            rr[N][2] = r[s + 2 * np];
+        }
+    });
     copy_wait();
     __syncthreads();
-    tile_phase<T, KIND, ELASTIC, SPARSE, 0>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, B, r, xout);
+    tile_phase<T, KIND, ELASTIC, SPARSE, 0>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, sbase, rr[0], xout);
     __syncthreads();
-    tile_phase<T, KIND, ELASTIC, SPARSE, 1>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, B, r, xout);
+    tile_phase<T, KIND, ELASTIC, SPARSE, 1>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, sbase, rr[1], xout);
     __syncthreads();
-    tile_phase<T, KIND, ELASTIC, SPARSE, 2>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, B, r, xout);
+    tile_phase<T, KIND, ELASTIC, SPARSE, 2>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, sbase, rr[2], xout);
     __syncthreads();
-    tile_phase<T, KIND, ELASTIC, SPARSE, 3>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, B, r, xout);
+    tile_phase<T, KIND, ELASTIC, SPARSE, 3>(g, c, k, i0, j0, zin, has_lo, has_hi, op, cf, sbase, rr[3], xout);
 }
 
-// res = r - A x on one 32x32 tile of plane k (all 4 colours of the plane),
-// from the same staged planes; every node's arithmetic is that of the
-// residual kernel (const_row / plane_row_coef with the centre block, ops.cuh).
-// With NORM each CTA writes the FP64 sum of |res|^2 over its tile to
+// res = r - A x at one node of x-parity A (the arithmetic of the residual
+// kernel: const_row / plane_row_coef with the centre block, ops.cuh).
+template <typename T, int KIND, bool ELASTIC, bool SPARSE, int A>
+__device__ __forceinline__ void res_node(const LevelOp<T> &op, const T *cf, const unsigned (&cz)[3], bool zin,
+                                         bool has_lo, bool has_hi, T *acc) {
+    if (KIND == OP_CONST) {
+        if (zin) {
+            tile_const_row<T, ELASTIC, true, A, kRowsRes>(op.cop, cz, acc);
+        } else {
+            T v[3];
+            lds<nb_off<A, kRowsRes>(13, 0)>(cz[1], v[0]);
+            lds<nb_off<A, kRowsRes>(13, 1)>(cz[1], v[1]);
+            lds<nb_off<A, kRowsRes>(13, 2)>(cz[1], v[2]);
+            matvec_sub(op.cop.fix, v, acc);
+        }
+    } else {
+        tile_plane_row<T, SPARSE, true, A, kRowsRes>(cf, cz, has_lo, has_hi, acc);
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void copy_wait_but() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void copy_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+// Ring slots of the marching residual: planes k-1, k, k+1 in use and k+2 in
+// flight; r of planes k and k+1 in a second ring after them.
+constexpr int kRing = 4;
+constexpr int kRingSlot = 3 * kRowsRes * RS;   // words per slot
+// r of one plane of the tile: per component and colour 16 rows of 16 slots,
+// colours kRColour words apart (16 mod 32: the two half-warps of a warp, two
+// colours apart, fall on disjoint banks in FP32)
+constexpr int kRColour = 16 * 16 + 8;
+constexpr int kRSlot = 3 * 4 * kRColour;
+constexpr int kMarchSmemWords = kRing * kRingSlot + 2 * kRSlot;
+
+// Issue the copies of r of plane k of tile (tx, ty) into the r slot at shared
+// byte address d: 3 components x 4 colours x 16 rows x 4 chunks of 16 bytes.
+template <typename T>
+__device__ __forceinline__ void stage_r(const Geom &g, const T *__restrict__ r, int k, int tx, int ty, unsigned d) {
+    constexpr int E = 16 / sizeof(T), CPR = 16 / E;   // elements per chunk, chunks per row
+    for (int idx = threadIdx.x; idx < 3 * 4 * 16 * CPR; idx += kTileThreads) {
+        const int ch = idx % CPR, row = (idx / CPR) % 16, n = (idx / (CPR * 16)) % 4, cc = idx / (CPR * 64);
+        const size_t gs = (size_t)cc * g.npad + (size_t)(n + 4 * (k & 1)) * g.S +
+                          (size_t)((k >> 1) * g.N2 + ty * 16 + row) * g.M2 + tx * 16 + ch * E;
+        copy16_async(d + (unsigned)(((cc * 4 + n) * kRColour + row * 16 + ch * E) * (int)sizeof(T)), r + gs);
+    }
+}
+template <typename T>
+constexpr int kMarchMinBlocks = sizeof(T) == 4 ? 2 : 1;
+
+// res = r - A x on one 32x32 tile column, planes k0 .. k0 + zlen - 1: the CTA
+// marches up z with the planes in a ring of shared-memory slots, and the
+// copies of plane k + 2 are in flight while plane k is computed.  With NORM
+// each CTA writes the FP64 sum of |res|^2 over its nodes to
 // partial[CTA index].
 template <typename T, int KIND, bool ELASTIC, bool SPARSE, bool NORM>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, kMarchMinBlocks<T>)
     residual_tile_kernel(Geom g, const __grid_constant__ LevelOp<T> op, const T *__restrict__ r,
-                         const T *__restrict__ x, T *__restrict__ res, double *__restrict__ partial) {
+                         const T *__restrict__ x, T *__restrict__ res, double *__restrict__ partial, int zlen) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileBuf<T> &B = *reinterpret_cast<TileBuf<T> *>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     __shared__ T cf[KIND == OP_PLANE ? 252 : 1];
     const int ntx = g.m / kTX;
     const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
-    const int k = (int)blockIdx.y;
+    const int k0 = (int)blockIdx.y * zlen, k1 = min(g.o, k0 + zlen);
     const int i0 = tx * kTX - kHalo, j0 = ty * kTY - kHalo;
-    const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
-    const bool zin = g.zp || (k != 0 && k != g.o - 1);
-    if (KIND == OP_PLANE)
-        for (int e = threadIdx.x; e < 252; e += kTileThreads)
-            cf[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
-    // only the rows one beyond the tile are read
-    const int w0 = (i0 >> 1) - kHOff;
-    constexpr int JLO = kHalo - 1, NR = kTY + 2;
-    stage_plane<T, JLO, NR>(g, x, k, w0, j0, B, 1);
-    if (has_lo && (KIND == OP_PLANE || zin))
-        stage_plane<T, JLO, NR>(g, x, k == 0 ? g.o - 1 : k - 1, w0, j0, B, 0);
-    if (has_hi && (KIND == OP_PLANE || zin))
-        stage_plane<T, JLO, NR>(g, x, k == g.o - 1 ? 0 : k + 1, w0, j0, B, 2);
-    copy_wait();
-    __syncthreads();
-    constexpr int RS = 2 * kHW, CS = kSY * RS;
     const size_t np = (size_t)g.npad;
-    const int c = k & 1, K = k >> 1;
-    T *const flat = &B.v[0][0][0][0][0];
+    // plane kk (k0 - 1 <= kk <= k1) exists, its index, its slot
+    auto exists = [&](int kk) { return g.zp || (kk >= 0 && kk < g.o); };
+    auto wrapk = [&](int kk) { return kk < 0 ? kk + g.o : (kk >= g.o ? kk - g.o : kk); };
+    auto slot = [&](int kk) { return sbase + (unsigned)(((kk + kRing) % kRing) * kRingSlot * (int)sizeof(T)); };
+
+    auto rslot = [&](int kk) { return sbase + (unsigned)((kRing * kRingSlot + (kk & 1) * kRSlot) * (int)sizeof(T)); };
+
+    // cp.async groups: {x of k0-1, k0, k0+1; r of k0}, {x of k0+2; r of k0+1},
+    // then one per plane k: {x of k+3; r of k+2}
+    Stager<T, kRes0, kRowsRes, kRes0, kRowsRes> st;
+    st.init(g, (i0 >> 1) - kHOff, j0);
+    for (int kk = k0 - 1; kk <= k0 + 1; kk++)
+        if (kk <= k1 && exists(kk)) st.stage(g, x, wrapk(kk), slot(kk));
+    stage_r(g, r, k0, tx, ty, rslot(k0));
+    copy_commit();
+    if (k0 + 2 <= k1 && exists(k0 + 2)) st.stage(g, x, wrapk(k0 + 2), slot(k0 + 2));
+    if (k0 + 1 < k1) stage_r(g, r, k0 + 1, tx, ty, rslot(k0 + 1));
+    copy_commit();
+
+    // This thread's nodes: x-parity a, row parity b and column xs are the same
+    // in every plane; rows jj = kHalo + b + 2 (pr0 + 4 it), it = 0 .. 3.  A
+    // warp takes the 16 nodes of one x-parity in two adjacent rows (row stride
+    // 2 kHW words: the two half-warps fall on disjoint shared-memory banks in
+    // FP32); colour (a, b) with b the row parity.
+    const int xs = threadIdx.x & 15, b = (threadIdx.x >> 4) & 1, a = (threadIdx.x >> 5) & 1;
+    const int pr0 = threadIdx.x >> 6;
+    const int ii = kHalo + a + 2 * xs, i = wrapn(i0 + ii, g.m);
+    constexpr int NIT = kTX * kTY / kTileThreads;
+    static_assert(kTileThreads % 64 == 0 && NIT == 4, "node mapping");
     double sq = 0.0;
-    // A warp takes the 16 nodes of one x-parity a in two adjacent rows (row
-    // stride 2 kHW words: the two half-warps fall on disjoint shared-memory
-    // banks in FP32); colour (a, b) with b the row parity.
-    for (int t = threadIdx.x; t < kTX * kTY; t += kTileThreads) {
-        const int xs = t & 15, b = (t >> 4) & 1, a = (t >> 5) & 1, pr = t >> 6;
-        const int ii = kHalo + a + 2 * xs, jj = kHalo + b + 2 * pr;
-        const int i = wrapn(i0 + ii, g.m), j = wrapn(j0 + jj, g.n);
-        const int q = a + 2 * b + 4 * c;
-        const int s = q * g.S + (K * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
-        T acc[3] = {r[s], r[s + np], r[s + 2 * np]};
-        const T *self = flat + 3 * CS + jj * RS + a * kHW + (ii >> 1) + kHOff;
-        auto fetch = [&](int bb, int cc) -> T {
-            const int dx = bdx(bb), dy = bdy(bb), dz = bdz(bb);
-            return self[(dz * 3 + cc) * CS + dy * RS + (((a + dx) & 1) - a) * kHW + ((a + dx) >> 1)];
+    for (int k = k0; k < k1; k++) {
+        if (KIND == OP_PLANE)
+            for (int e = threadIdx.x; e < 252; e += kTileThreads)
+                cf[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+        copy_wait_but<1>();   // every group but the newest ({x of k+2; r of k+1}) has landed
+        __syncthreads();
+        const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
+        const bool zin = g.zp || (k != 0 && k != g.o - 1);
+        const unsigned rs = rslot(k) + (unsigned)(((a + 2 * b) * kRColour + xs) * (int)sizeof(T));
+        const unsigned s0 = slot(k - 1), s1 = slot(k), s2 = slot(k + 1);
+        auto node = [&](int it) {
+            const int jj = kHalo + b + 2 * (pr0 + 4 * it);
+            const int j = wrapn(j0 + jj, g.n);
+            const int s = (a + 2 * b + 4 * (k & 1)) * g.S + ((k >> 1) * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
+            T acc[3];
+            const unsigned ra = rs + (unsigned)((pr0 + 4 * it) * 16 * (int)sizeof(T));
+            lds<0>(ra, acc[0]);
+            lds<4 * kRColour>(ra, acc[1]);
+            lds<8 * kRColour>(ra, acc[2]);
+            const unsigned cw = (unsigned)(corner_word<kRes0>(ii, jj) * (int)sizeof(T));
+            const unsigned cz[3] = {s0 + cw, s1 + cw, s2 + cw};
+            if (a == 0) res_node<T, KIND, ELASTIC, SPARSE, 0>(op, cf, cz, zin, has_lo, has_hi, acc);   // warp-uniform
+            else res_node<T, KIND, ELASTIC, SPARSE, 1>(op, cf, cz, zin, has_lo, has_hi, acc);
+            res[s] = acc[0];
+            res[s + np] = acc[1];
+            res[s + 2 * np] = acc[2];
+            if (NORM)
+                sq += (double)acc[0] * (double)acc[0] + (double)acc[1] * (double)acc[1] + (double)acc[2] * (double)acc[2];
         };
-        if (KIND == OP_CONST) {
-            if (zin) {
-                // const_row<T, ELASTIC, true>
-                T v[27][3];
+        if constexpr (KIND == OP_CONST && ELASTIC) {
 #pragma unroll
-                for (int bb = 0; bb < 27; bb++) {
-                    if (ELASTIC && nnz_axes(bb) == 3) continue;
-#pragma unroll
-                    for (int cc = 0; cc < 3; cc++) {
-                        bool used = !ELASTIC || bb == 13;
-#pragma unroll
-                        for (int rr = 0; rr < 3; rr++) used = used || elastic_entry(bb, 3 * rr + cc);
-                        v[bb][cc] = used ? fetch(bb, cc) : T(0);
-                    }
-                }
-#pragma unroll
-                for (int bb = 0; bb < 27; bb++) {
-                    if (ELASTIC && nnz_axes(bb) == 3) continue;
-                    if (ELASTIC && bb != 13) {
-#pragma unroll
-                        for (int e = 0; e < 9; e++)
-                            if (elastic_entry(bb, e)) acc[e / 3] -= op.cop.a[bb][e] * v[bb][e % 3];
-                    } else if (bb == 13 && op.cop.centre_diag) {
-                        acc[0] -= op.cop.a[13][0] * v[13][0];
-                        acc[1] -= op.cop.a[13][4] * v[13][1];
-                        acc[2] -= op.cop.a[13][8] * v[13][2];
-                    } else {
-                        matvec_sub(op.cop.a[bb], v[bb], acc);
-                    }
-                }
-            } else {
-                T v[3] = {self[0], self[CS], self[2 * CS]};
-                matvec_sub(op.cop.fix, v, acc);
-            }
+            for (int it = 0; it < NIT; it++) node(it);
         } else {
-            // plane_row_coef<T, SPARSE, true>: all 27 blocks, none beyond a Dirichlet z-boundary
-#pragma unroll
-            for (int bb = 0; bb < 27; bb++) {
-                asm volatile("" ::: "memory");
-                const bool out = (bdz(bb) < 0 && !has_lo) || (bdz(bb) > 0 && !has_hi);
-                T vv[3];
-#pragma unroll
-                for (int cc = 0; cc < 3; cc++) vv[cc] = out ? T(0) : fetch(bb, cc);
-#pragma unroll
-                for (int e = 0; e < 9; e++)
-                    if (!SPARSE || coarse_entry(bb, e)) acc[e / 3] -= cf[9 * bb + e] * vv[e % 3];
-            }
+            // a full-block row is long: unrolling the four nodes would spill
+#pragma unroll 1
+            for (int it = 0; it < NIT; it++) node(it);
         }
-        res[s] = acc[0];
-        res[s + np] = acc[1];
-        res[s + 2 * np] = acc[2];
-        if (NORM) sq += (double)acc[0] * (double)acc[0] + (double)acc[1] * (double)acc[1] + (double)acc[2] * (double)acc[2];
+        __syncthreads();   // x slot of plane k - 1, r slot of plane k (and cf) free
+        if (k + 3 <= k1 && exists(k + 3)) st.stage(g, x, wrapk(k + 3), slot(k + 3));
+        if (k + 2 < k1) stage_r(g, r, k + 2, tx, ty, rslot(k + 2));
+        copy_commit();
     }
+    copy_wait_but<0>();
     if (NORM) {
         __shared__ double red[kTileThreads / 32];
 #pragma unroll
@@ -346,15 +513,33 @@ void launch_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin
     }
     for (int c = 0; c < 2; c++) {
         const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
-        if (planes > 0) kern<<<dim3(tiles, planes), kTileThreads, smem, st>>>(g, c, op, r, xin, xout);
+        if (planes > 0) kern<<<dim3(tiles, planes), kGsThreads, smem, st>>>(g, c, op, r, xin, xout);
     }
+}
+
+// Planes per CTA of the marching residual: about four waves of CTAs over the
+// SMs (each CTA also stages the two planes beyond its chunk), 4 .. 32 planes.
+template <typename T>
+int march_zlen(const Geom &g) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long tiles = (long)(g.m / kTX) * (g.n / kTY);
+    const long per = 4L * sms * kMarchMinBlocks<T>;
+    const long z = (g.o * tiles + per - 1) / per;
+    return (int)std::min<long>(32, std::max<long>(4, z));
 }
 
 template <typename T, int KIND, bool ELASTIC, bool SPARSE>
 void launch_res_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, double *partial,
                        cudaStream_t st) {
-    const int smem = (int)sizeof(TileBuf<T>);
-    const dim3 grid((g.m / kTX) * (g.n / kTY), g.o);
+    const int smem = kMarchSmemWords * (int)sizeof(T);
+    const int zlen = march_zlen<T>(g);
+    const dim3 grid((g.m / kTX) * (g.n / kTY), (g.o + zlen - 1) / zlen);
     static bool attr_set = false;   // per instantiation
     if (!attr_set) {
         cudaFuncSetAttribute(residual_tile_kernel<T, KIND, ELASTIC, SPARSE, false>,
@@ -364,9 +549,11 @@ void launch_res_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T 
         attr_set = true;
     }
     if (partial)
-        residual_tile_kernel<T, KIND, ELASTIC, SPARSE, true><<<grid, kTileThreads, smem, st>>>(g, op, r, x, res, partial);
+        residual_tile_kernel<T, KIND, ELASTIC, SPARSE, true>
+            <<<grid, kTileThreads, smem, st>>>(g, op, r, x, res, partial, zlen);
     else
-        residual_tile_kernel<T, KIND, ELASTIC, SPARSE, false><<<grid, kTileThreads, smem, st>>>(g, op, r, x, res, partial);
+        residual_tile_kernel<T, KIND, ELASTIC, SPARSE, false>
+            <<<grid, kTileThreads, smem, st>>>(g, op, r, x, res, partial, zlen);
 }
 
 }  // namespace
@@ -401,23 +588,24 @@ void launch_gs_sweep_tile(const LevelOp<T> &op, const Geom &g, const T *r, const
 }
 
 // Where the tiled residual runs.  Measured on a GB300 (256x256x257 problem,
-// FP32): on the plane-invariant level 1 it beats the colour-interleaved
-// residual kernel 63.6 vs 165.5 us (that kernel re-reads the plane's 252
-// coefficients per node from global memory); on the fine shared-stencil level
-// it loses (251.5 vs 223.2 us), so by default it runs on FP32 plane-invariant
-// levels of at least 64x64 nodes per plane.  STZ_MG_TILE=0 disables it,
-// STZ_MG_TILE=1 uses it wherever it applies, FP64 included.
+// FP32): 167 vs 223 us on the fine shared-stencil level and 72 vs 166 us on
+// the plane-invariant level 1 against the colour-interleaved residual kernel,
+// so by default it runs on FP32 levels of at least 64x64 nodes per plane.
+// STZ_MG_TILE=0 disables it, STZ_MG_TILE=1 uses it in FP64 too.
 template <typename T>
 bool residual_tile_applies(const LevelOp<T> &op, const Geom &g) {
     int mode = -1;
     if (const char *e = std::getenv("STZ_MG_TILE")) mode = std::atoi(e) != 0;
     if (mode == 0) return false;
     if (op.kind != OP_CONST && op.kind != OP_PLANE) return false;
-    if (mode < 0 && (sizeof(T) != 4 || op.kind != OP_PLANE)) return false;
+    if (mode < 0 && sizeof(T) != 4) return false;
     return g.xp && g.yp && g.m % kTX == 0 && g.n % kTY == 0 && g.m * g.n >= 64 * 64;
 }
 
-int residual_tile_blocks(const Geom &g) { return (g.m / kTX) * (g.n / kTY) * g.o; }
+int residual_tile_blocks(const Geom &g, bool fp64) {
+    const int zlen = fp64 ? march_zlen<double>(g) : march_zlen<float>(g);
+    return (g.m / kTX) * (g.n / kTY) * ((g.o + zlen - 1) / zlen);
+}
 
 template <typename T>
 void launch_residual_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, double *partial,
