@@ -47,18 +47,18 @@ template <typename T>
 constexpr int kTileMinBlocks = sizeof(T) == 4 ? 3 : 1;
 // Threads of the tiled sweep: every phase (at most 19 x 19 nodes) in one round.
 constexpr int kGsThreads = 384;
-constexpr int RS = 2 * kHW;   // words per row of one component plane
-constexpr int CS = kSY * RS;  // words per component plane
-constexpr int PS = 3 * CS;    // words per buffer plane
+constexpr int RS = 2 * kHW;   // words per row (both x-parities) of one component plane
 
 __device__ __forceinline__ int wrapn(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 // Three planes (k-1, k, k+1) of the widened tile, 3 components each, every
-// row split by the parity of x so that a warp working on one colour reads
-// consecutive words: node ii of row jj is at [..][jj][ii & 1][(ii >> 1) + kHOff].
+// component plane split by the parity of x so that a warp working on one
+// colour reads consecutive words: node ii of row jj is at
+// [..][ii & 1][jj][(ii >> 1) + kHOff].  Rows of one parity are kHW = 24 words
+// apart, so two rows of one colour (2 kHW apart) fall on banks 16 apart.
 template <typename T>
 struct TileBuf {
-    T v[3][3][kSY][2][kHW];
+    T v[3][3][2][kSY][kHW];
 };
 
 // Rows of one buffer component plane: the sweep stages rows 0 .. kSY - 1 of
@@ -68,18 +68,18 @@ constexpr int kRowsRes = kTY + 2, kRes0 = kHalo - 1;
 
 // A node's neighbours in one buffer plane are read relative to its "corner"
 // word there: row jj - 1, slot (ii >> 1) + kHOff - 1 of the x-parity-0
-// half-row.  Neighbour (bdx, bdy)(b), component c, of a node of x-parity A is
+// half-plane.  Neighbour (bdx, bdy)(b), component c, of a node of x-parity A is
 // then at this non-negative compile-time word offset, in a buffer plane of
 // NROWS rows per component (the node itself: b = 13, in its own plane).
 template <int A, int NROWS>
 __host__ __device__ constexpr int nb_off(int b, int c) {
-    return c * NROWS * RS + (bdy(b) + 1) * RS + ((A + bdx(b) + 2) & 1) * kHW + ((A + bdx(b) + 2) >> 1);
+    return c * NROWS * RS + ((A + bdx(b) + 2) & 1) * NROWS * kHW + (bdy(b) + 1) * kHW + ((A + bdx(b) + 2) >> 1);
 }
 
 // Corner word of node (ii, jj) in a buffer plane whose row 0 is tile row ROW0.
 template <int ROW0>
 __device__ __forceinline__ int corner_word(int ii, int jj) {
-    return (jj - 1 - ROW0) * RS + (ii >> 1) + kHOff - 1;
+    return (jj - 1 - ROW0) * kHW + (ii >> 1) + kHOff - 1;
 }
 
 // Shared-memory load / store at a compile-time byte offset from a 32-bit
@@ -147,7 +147,7 @@ struct Stager {
                 const int j = wrapn(j0 + jj, g.n);
                 const int I = wrapn(w0 + cn * E, g.M2);    // a chunk never straddles the wrap (M2 % E == 0)
                 goff[d] = (((j & 1) << 1) + p) * g.S + (j >> 1) * g.M2 + I;
-                soff[d] = (unsigned)((((jj - ROW0) * 2 + p) * kHW + cn * E) * (int)sizeof(T));
+                soff[d] = (unsigned)(((p * NROWS + jj - ROW0) * kHW + cn * E) * (int)sizeof(T));
             }
         }
     }
@@ -432,16 +432,15 @@ __global__ void __launch_bounds__(kTileThreads, kMarchMinBlocks<T>)
     if (k0 + 1 < k1) stage_r(g, r, k0 + 1, tx, ty, rslot(k0 + 1));
     copy_commit();
 
-    // This thread's nodes: x-parity a, row parity b and column xs are the same
-    // in every plane; rows jj = kHalo + b + 2 (pr0 + 4 it), it = 0 .. 3.  A
-    // warp takes the 16 nodes of one x-parity in two adjacent rows (row stride
-    // 2 kHW words: the two half-warps fall on disjoint shared-memory banks in
-    // FP32); colour (a, b) with b the row parity.
-    const int xs = threadIdx.x & 15, b = (threadIdx.x >> 4) & 1, a = (threadIdx.x >> 5) & 1;
-    const int pr0 = threadIdx.x >> 6;
+    // This thread's nodes: colour (a, b) and column xs are the same in every
+    // plane; rows jj = kHalo + b + 2 R with R = h + 2 q2 + 4 it, it = 0 .. 3.
+    // A warp takes 16 nodes of one colour in each of two rows 2 apart (2 kHW
+    // words: the two half-warps fall on disjoint shared-memory banks in FP32).
+    const int xs = threadIdx.x & 15, h = (threadIdx.x >> 4) & 1, a = (threadIdx.x >> 5) & 1;
+    const int b = (threadIdx.x >> 6) & 1, pr0 = h + 2 * (threadIdx.x >> 7);
     const int ii = kHalo + a + 2 * xs, i = wrapn(i0 + ii, g.m);
     constexpr int NIT = kTX * kTY / kTileThreads;
-    static_assert(kTileThreads % 64 == 0 && NIT == 4, "node mapping");
+    static_assert(kTileThreads == 256 && NIT == 4, "node mapping");
     double sq = 0.0;
     for (int k = k0; k < k1; k++) {
         if (KIND == OP_PLANE)
@@ -454,7 +453,7 @@ __global__ void __launch_bounds__(kTileThreads, kMarchMinBlocks<T>)
         const unsigned rs = rslot(k) + (unsigned)(((a + 2 * b) * kRColour + xs) * (int)sizeof(T));
         const unsigned s0 = slot(k - 1), s1 = slot(k), s2 = slot(k + 1);
         auto node = [&](int it) {
-            const int jj = kHalo + b + 2 * (pr0 + 4 * it);
+            const int jj = kHalo + b + 2 * (pr0 + 4 * it);   // row R = pr0 + 4 it
             const int j = wrapn(j0 + jj, g.n);
             const int s = (a + 2 * b + 4 * (k & 1)) * g.S + ((k >> 1) * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
             T acc[3];

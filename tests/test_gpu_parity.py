@@ -194,22 +194,23 @@ def test_reference_hierarchy_gs_bottom(oracle_port):
 
 
 
-TILE_LEVEL_CASES = [((64, 64, 17), (True, True, False), 0, 2), ((64, 64, 16), (True, True, True), 0, 2),
-                    ((96, 64, 9), (True, True, False), 0, 4), ((128, 128, 17), (True, True, False), 1, 2),
-                    ((128, 128, 16), (True, True, True), 1, 3)]
+TILE_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64, 16), (True, True, True), "const", 0, 2),
+                    ((96, 64, 9), (True, True, False), "const", 0, 4), ((128, 128, 17), (True, True, False), "const", 1, 2),
+                    ((128, 128, 16), (True, True, True), "const", 1, 3), ((64, 64, 17), (True, True, False), "trans", 0, 2),
+                    ((64, 64, 16), (True, True, True), "trans", 0, 3), ((128, 128, 17), (True, True, False), "trans", 1, 2)]
 
 
-@pytest.mark.parametrize("dims,per,level,sweeps", TILE_LEVEL_CASES)
-def test_tiled_sweep_is_the_colour_sweep(dims, per, level, sweeps, monkeypatch):
+@pytest.mark.parametrize("dims,per,kind,level,sweeps", TILE_LEVEL_CASES)
+def test_tiled_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, monkeypatch):
     """The tiled two-buffer sweep (each CTA runs a plane tile's four colours
     from shared memory, recomputing a 4-node halo) gives bit-for-bit the
-    result of the eight colour launches: FP64 level sweeps of the shared
-    stencil and of a plane-invariant coarse operator, Dirichlet and periodic
-    z, even and odd sweep counts."""
+    result of the eight colour launches: FP64 level sweeps of the elastic and
+    of a full non-symmetric shared stencil and of their plane-invariant
+    coarse operators, Dirichlet and periodic z, even and odd sweep counts."""
     import stzpp_gb300 as sg
     m, n, o = dims
     dx, dy, dz = P.grid_spacing(m, n, o, per)
-    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz)
+    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz) if kind == "const" else trans_stencil(2, dx)
     out = {}
     for tile in ("0", "1"):
         monkeypatch.setenv("STZ_MG_TILE", tile)
