@@ -539,15 +539,142 @@ def run_coeff_change(args, local, steps=12):
     print(json.dumps(line), flush=True)
 
 
+# Algorithmic bytes of one advection step per interior cell: read u, v, w,
+# the 6 stresses, chi, the previous ad_Dpl and cchi; write the 6 stress
+# changes, cchi, sbar and ad_Dpl (21 doubles).
+ADV_BYTES_PER_CELL = 21 * 8
+
+
+def advection_fields(n, seed, device):
+    """Seeded fields of an n^3 ghosted grid, made on the device: velocities
+    N(0, 1e-3); stress tensors of random direction scaled to a deviatoric
+    magnitude sbar ~ U(0.5, 1.15) (in units of the yield stress: about 23 % of
+    the cells above it, as in a shear band of a running simulation); chi about
+    550 K; previous ad_Dpl U(0, 1e-3); ghosts periodic in x and y, random in z."""
+    import torch
+    from stzpp_gb300 import advect
+    g = advect.NGHOST
+    gen = torch.Generator(device=device).manual_seed(seed)
+    shape = (n + 2 * g,) * 3
+    f = {}
+    for k in advect.INPUTS + advect.OUTPUTS:
+        t = torch.zeros(shape, dtype=torch.float64, device=device)
+        if k in ("u", "v", "w"):
+            t.normal_(0, 1e-3, generator=gen)
+        elif k.startswith("s") and k != "sbar":
+            t.normal_(0, 1.0, generator=gen)
+        elif k == "chi":
+            t.normal_(550 / 21000, 15 / 21000, generator=gen)
+        elif k == "ad_dpl":
+            t.uniform_(0, 1e-3, generator=gen)
+        f[k] = t
+    p = -(f["s11"] + f["s22"] + f["s33"]) / 3
+    dev = torch.sqrt(0.5 * ((f["s11"] + p) ** 2 + (f["s22"] + p) ** 2 + (f["s33"] + p) ** 2) +
+                     f["s12"] ** 2 + f["s13"] ** 2 + f["s23"] ** 2)
+    target = torch.empty(shape, dtype=torch.float64, device=device).uniform_(0.5, 1.15, generator=gen)
+    scale = target / dev
+    for k in ("s11", "s12", "s13", "s22", "s23", "s33"):
+        f[k] *= scale
+    for k, t in f.items():
+        t[:, :, :g] = t[:, :, n:n + g]
+        t[:, :, n + g:] = t[:, :, g:2 * g]
+        t[:, :g] = t[:, n:n + g]
+        t[:, n + g:] = t[:, g:2 * g]
+        f[k] = t.reshape(-1)
+    return f
+
+
+def run_advection(args, local, n=256, dt=200.0):
+    """The quasi-static advection step of shear_sim_3d (the part of a
+    step_forward_qs before the projection solve) on a 256^3-cell grid at the
+    reference driver's quasi-static step (dt = tf / N_tp / qs_steps = 4e5 /
+    200 / 10, shear_sim.cpp:58-60): ms per step with the fields resident in
+    HBM, and end to end with the inputs copied from pinned host memory and the
+    outputs copied back every step."""
+    import torch
+    torch.cuda.set_device(local)
+    sys.path.insert(0, ROOT)
+    from oracle import advect as A
+    from stzpp_gb300 import advect
+    dims = (n, n, n)
+    sp = (1.0 / n,) * 3
+    prm = A.driver_params(n)
+    f = advection_fields(n, 0, f"cuda:{local}")
+    work = torch.empty(advect.work_size(*dims), dtype=torch.float64, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    yielded = advect.advection_step(f, dims, sp, prm, dt, work=work)
+    plastic = float((f["ad_dpl"].reshape((n + 4,) * 3)[2:-2, 2:-2, 2:-2] > 0).double().mean())
+    for _ in range(args.warmup):
+        advect.advection_step(f, dims, sp, prm, dt, work=work, wait=False)
+    clocks = Clocks(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        advect.advection_step(f, dims, sp, prm, dt, work=work, wait=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    # end to end: every step copies the 12 input fields in and the 9 changed ones out
+    ins = list(advect.INPUTS) + ["ad_dpl", "cchi"]
+    host_in = {k: torch.empty_like(f[k], device="cpu").pin_memory() for k in ins}
+    host_out = {k: torch.empty_like(f[k], device="cpu").pin_memory() for k in advect.OUTPUTS}
+    for k in ins:
+        host_in[k].copy_(f[k])
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        for k in ins:
+            f[k].copy_(host_in[k], non_blocking=True)
+        advect.advection_step(f, dims, sp, prm, dt, work=work, wait=False)
+        for k in advect.OUTPUTS:
+            host_out[k].copy_(f[k], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    npts = advect.grid_points(*dims)
+    # CPU baseline: the C restatement on a 48^3 sample of the same fields, scaled by cells
+    m = 48
+    fs = advection_fields(m, 0, f"cuda:{local}")
+    Fs = np.zeros((advect.grid_points(m, m, m), A.NFIELD))
+    for k, c in (("u", A.U), ("v", A.V), ("w", A.W), ("s11", A.S11), ("s12", A.S12), ("s13", A.S13),
+                 ("s22", A.S22), ("s23", A.S23), ("s33", A.S33), ("chi", A.CHI), ("ad_dpl", A.ADPL)):
+        Fs[:, c] = fs[k].cpu().numpy()
+    t0 = time.perf_counter()
+    A.port_step(Fs, m, m, m, A.driver_params(m), dt)
+    cpu_ms = (time.perf_counter() - t0) * 1e3 * (n / m) ** 3
+    peak, kind = peaks()
+    achieved = ADV_BYTES_PER_CELL * n ** 3 / (ms * 1e-3) / 1e9
+    line = {"metric": f"ms per quasi-static advection step (shear_sim_3d::advection_step), {n}^3 cells",
+            "value": ms, "unit": "ms", "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup,
+            "config": {"workload": f"{n}^3 interior cells, 2 ghost layers (periodic x,y), the reference driver's "
+                                   f"STZ parameters and quasi-static step dt = {dt}, velocities N(0,1e-3), stress "
+                                   "magnitudes sbar ~ U(0.5, 1.15) sy (seed 0); inputs (2.6 GB) larger than L2",
+                       "plastic_fraction": plastic, "yielded": yielded},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "bytes_per_cell": ADV_BYTES_PER_CELL, "peak_kind": kind},
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 8 * npts * len(ins),
+                    "d2h_bytes_per_step": 8 * npts * len(advect.OUTPUTS)},
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": f"C restatement of the step on {m}^3 cells of the same kind, scaled by cell count"},
+            "gpu_launches": 3 * args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", type=int, choices=[2, 3, 5, 6], default=2,
+    ap.add_argument("--config", type=int, choices=[2, 3, 5, 6, 7], default=2,
                     help="2: the 256x256x257 headline solve (default); 3: 512x512x257 variable mu, mixed vs FP64; "
-                         "5: 50-solve sequence with checkpointed backward; 6: per-step coefficient change")
+                         "5: 50-solve sequence with checkpointed backward; 6: per-step coefficient change; "
+                         "7: the quasi-static advection step on 256^3 cells")
+    ap.add_argument("--cells", type=int, default=256, help="cells per dimension of the advection workload (--config 7)")
     ap.add_argument("--max-coarse", type=int, default=1024,
                     help="hierarchy stop rule of the headline solve (reference: 1024 nodes)")
     args = ap.parse_args()
@@ -558,6 +685,8 @@ def main():
         run_config5(args, local)
     elif args.config == 6 and args.impl == "ours":
         run_coeff_change(args, local)
+    elif args.config == 7 and args.impl == "ours":
+        run_advection(args, local, n=args.cells)
     elif args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -233,6 +233,48 @@ int stz_mg_const_residual_sumsq_noalloc(int m, int n, int o, int x_prd, int y_pr
                                         const double *stencil, const double *fix, const double *x,
                                         const double *b, double *sumsq, int device, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Quasi-static advection step (shear_sim_3d::advection_step,
+ * src/shear_sim_3d.cpp:393-525, with advection_grid_step :409-525,
+ * adaptive_plastic_term :108-147, chi_diffusion :1216-1236, eno2
+ * :1256-1266): the part of step_forward_qs (:381-389) before merge_updates and
+ * the projection solve, on the device.
+ *
+ * Every field is a device array over the reference's ghosted grid of
+ * (nx + 4) x (ny + 4) x (nz + 4) points (nghost = 2, shear_sim_3d.cpp:39-49,
+ * 81-82), x fastest, one array per Field member (src/field.hh:11-22); the
+ * ghost layers are inputs, filled by the caller as set_up_ghost_regions and
+ * set_boundary_conditions fill them.  For every interior point the step
+ * writes sbar (Field::dev), the stress changes cs11..cs33, adds the chi
+ * change to cchi (the reference's +=) and replaces ad_Dpl; a point's chi
+ * diffusion sees the new ad_Dpl of its interior -x, -y, -z neighbours and the
+ * old one of the others, as the reference's in-place sweep does.
+ * work: 2 x (ghosted points) + 2 doubles of scratch.  Asynchronous on
+ * `stream` (a cudaStream_t, NULL: the default stream) unless yielded is
+ * non-NULL: then the call waits and sets *yielded to 1 if some point reached
+ * the yield stress (the reference's "Starting to reach the yield stress"
+ * message), and returns STZ_MG_ERR_NONFINITE if a point's adaptive plastic
+ * sub-stepping did not finish within 2^22 sub-steps. */
+typedef struct {
+    int nx, ny, nz;     /* interior points */
+    double dx, dy, dz;  /* grid spacing */
+    /* STZ parameters (shear_sim_3d.hh:120-136) */
+    double mu, sy, tau0, eps0, c0, delta, omega, bath_temp, chi_inf, ez, diff_l;
+} stz_adv_params;
+
+typedef struct {
+    const double *u, *v, *w;                       /* node velocities */
+    const double *s11, *s12, *s13, *s22, *s23, *s33; /* cell stresses */
+    const double *chi;                             /* effective temperature */
+    double *ad_dpl;                                /* in: previous step (every point); out: interior */
+    double *sbar;                                  /* out */
+    double *cs11, *cs12, *cs13, *cs22, *cs23, *cs33; /* out: stress changes */
+    double *cchi;                                  /* in/out: chi change */
+    double *work;                                  /* scratch */
+} stz_adv_fields;
+
+int stz_mg_advection_step(const stz_adv_params *p, const stz_adv_fields *f, double dt, void *stream, int *yielded);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,8 @@ int MPI_Comm_split(MPI_Comm comm, int color, int key, MPI_Comm *newcomm);
 int MPI_Cart_create(MPI_Comm comm, int ndims, const int *dims, const int *periods,
                     int reorder, MPI_Comm *cart);
 int MPI_Cart_rank(MPI_Comm comm, const int *coords, int *rank);
+int MPI_Cart_get(MPI_Comm comm, int maxdims, int *dims, int *periods, int *coords);
+int MPI_Cart_shift(MPI_Comm comm, int direction, int disp, int *source, int *dest);
 int MPI_Cart_coords(MPI_Comm comm, int rank, int maxdims, int *coords);
 int MPI_Isend(const void *buf, int count, MPI_Datatype type, int dest, int tag,
               MPI_Comm comm, MPI_Request *req);

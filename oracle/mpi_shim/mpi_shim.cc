@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -29,6 +30,7 @@ struct QueuedMsg {
 std::deque<PendingRecv> g_recvs;
 std::deque<QueuedMsg> g_msgs;
 int g_next_comm = 2;
+std::map<MPI_Comm, std::vector<int>> g_cart_periods;
 
 size_t type_size(MPI_Datatype t) {
     switch (t) {
@@ -61,10 +63,31 @@ int MPI_Comm_split(MPI_Comm, int color, int, MPI_Comm *newcomm) {
     return MPI_SUCCESS;
 }
 
-int MPI_Cart_create(MPI_Comm, int ndims, const int *dims, const int *, int, MPI_Comm *cart) {
+int MPI_Cart_create(MPI_Comm, int ndims, const int *dims, const int *periods, int, MPI_Comm *cart) {
     for (int d = 0; d < ndims; d++)
         if (dims[d] != 1) throw std::runtime_error("mpi shim: Cartesian grid must be 1x1x1");
     *cart = g_next_comm++;
+    std::vector<int> &p = g_cart_periods[*cart];
+    p.assign(periods, periods + ndims);
+    return MPI_SUCCESS;
+}
+
+// One rank: every dimension has extent 1 and coordinate 0.
+int MPI_Cart_get(MPI_Comm comm, int maxdims, int *dims, int *periods, int *coords) {
+    auto it = g_cart_periods.find(comm);
+    for (int d = 0; d < maxdims; d++) {
+        dims[d] = 1;
+        periods[d] = (it != g_cart_periods.end() && d < (int)it->second.size()) ? it->second[d] : 0;
+        coords[d] = 0;
+    }
+    return MPI_SUCCESS;
+}
+
+// The neighbours along a dimension: this rank itself if it is periodic, else none.
+int MPI_Cart_shift(MPI_Comm comm, int direction, int, int *source, int *dest) {
+    auto it = g_cart_periods.find(comm);
+    const bool per = it != g_cart_periods.end() && direction < (int)it->second.size() && it->second[direction];
+    *source = *dest = per ? 0 : MPI_PROC_NULL;
     return MPI_SUCCESS;
 }
 

@@ -40,7 +40,7 @@ EXPORTS = (
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
     "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
-    "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update",
+    "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update", "stz_mg_advection_step",
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
@@ -104,6 +104,7 @@ def load_library():
     lib.stz_mg_adjoint_solve.argtypes = [vp, vp, vp, ci, cd, ci, ctypes.POINTER(ci), ctypes.POINTER(cd)]
     lib.stz_mg_coeff_grad.argtypes = [vp, vp, vp, vp, vp, ci]
     lib.stz_mg_stress_update.argtypes = [vp, vp, cd, cd, cd, cd, cd, cd, ctypes.POINTER(cd), ci]
+    lib.stz_mg_advection_step.argtypes = [vp, vp, cd, vp, ctypes.POINTER(ci)]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci

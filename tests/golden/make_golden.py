@@ -23,7 +23,12 @@ Also ``trans``: the reference's transformed-frame stencils of trans_sim_3d
 for a few frames (the coefficient-change path), from its generated
 stenc_funcs.hh -> tests/golden/trans_stencils.npz.
 
-Run: python tests/golden/make_golden.py [trans]
+Also ``adv``: the reference's quasi-static advection step
+(shear_sim_3d::advection_step) run once through oracle/_ref/libstzadv.so
+(``make -C oracle advref``) on seeded ghosted grids -> tests/golden/adv_step.npz
+(inputs and the changed Field members of every point).
+
+Run: python tests/golden/make_golden.py [trans | adv]
 """
 import os
 import sys
@@ -107,7 +112,37 @@ def trans_stencils(path):
     print("wrote", path)
 
 
+# (name, interior dims, seed, dt, stress bias toward yield)
+ADV_CASES = [("elastic", (6, 5, 4), 3, 500.0, -0.5), ("mixed", (7, 6, 5), 0, 500.0, 0.0),
+             ("plastic", (6, 6, 4), 2, 50.0, 1.2), ("long", (5, 4, 6), 1, 2000.0, 0.6)]
+ADV_IN = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 19, 27]        # u v w s11..s33 chi cchi ad_Dpl
+ADV_OUT = [13, 14, 15, 16, 17, 18, 19, 26, 27]          # cs11..cs33 cchi sbar ad_Dpl
+
+
+def adv_steps(path):
+    from oracle import advect as A
+    if not A.reference_available():
+        sys.exit("oracle/_ref/libstzadv.so is missing: run `make -C oracle advref` where the reference is available")
+    out = {}
+    for name, (nx, ny, nz), seed, dt, bias in ADV_CASES:
+        prm = A.driver_params(nx)
+        F = A.random_fields(seed, nx, ny, nz, sigma_scale=0.7 if bias >= 0 else 0.2, plastic_bias=max(bias, 0.0))
+        R = A.reference_step(F, nx, ny, nz, prm, dt)
+        out[name + "/dims"] = np.array([nx, ny, nz])
+        out[name + "/dt"] = np.float64(dt)
+        out[name + "/params"] = np.array([prm[k] for k in A.PARAM_NAMES])
+        out[name + "/in"] = F[:, ADV_IN]
+        out[name + "/out"] = R[:, ADV_OUT]
+        print(name, "cells above the yield stress:", int((A.interior(R, nx, ny, nz)[..., 27] > 0).sum()),
+              "of", nx * ny * nz)
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "adv":
+        adv_steps(os.path.join(HERE, "adv_step.npz"))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "trans":
         trans_stencils(os.path.join(HERE, "trans_stencils.npz"))
         return
