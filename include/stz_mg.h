@@ -275,6 +275,44 @@ typedef struct {
 
 int stz_mg_advection_step(const stz_adv_params *p, const stz_adv_fields *f, double dt, void *stream, int *yielded);
 
+/* ------------------------------------------------------------------------
+ * Output in the reference's file formats, values made on the device.
+ *
+ * region::output_x / output_r / output_residual of the top level
+ * (mg_3d_template/region.cc:3062-3120) through region::output_internal
+ * (region.cc:3135-3202): the z-slice k of the solution x, the right-hand side
+ * r or the residual b - A x, written to `filename` as floats: {m, ax + i dx
+ * (i < m)}, then per row j {ay + j dy, m values}, dx = (bx-ax)/(m-1), dy =
+ * (by-ay)/(n-1) (the reference's default box is (0, m-1, 0, n-1)).  As in the
+ * reference, a vec3 value goes through vec3::operator double (src/vec3.hh:110,
+ * the squared magnitude): x and r slices hold float(|v|^2), the residual
+ * slice float(|r|^2 |r|^2). */
+enum { STZ_MG_SLICE_X = 0, STZ_MG_SLICE_R = 1, STZ_MG_SLICE_RESIDUAL = 2 };
+int stz_mg_output_slice(stz_mg_handle h, int which, int k, double ax, double bx, double ay, double by,
+                        const char *filename);
+
+/* shear_sim_3d::output_cube (src/shear_sim_3d.cpp:1961-2158) for one process:
+ * Field member `mode` (Field::fval, src/field.hh:157-177: 0-2 u v w, 3-8
+ * s11 s12 s13 s22 s23 s33, 9 pressure, 10 deviatoric stress, 11 chi,
+ * 12 chi*21000, 13-15 the reference map) of every interior point, x slowest
+ * and z fastest, as floats; the node-based members (0-2, 13-15) include the
+ * top z node (nz + 1 values per column).  Fields are device arrays over the
+ * ghosted grid of stz_mg_advection_step; members the mode does not read may
+ * be NULL.  stz_mg_cube_values writes the values to the device array `out`
+ * (asynchronous on `stream`); stz_mg_output_cube appends them to
+ * <dir>/<prefix>_grid.<frame>, creating dir if needed, as the reference does.
+ * Unlike the reference, mode 10 does not store sbar in the Field. */
+typedef struct {
+    const double *u, *v, *w;
+    const double *s11, *s12, *s13, *s22, *s23, *s33;
+    const double *chi;
+    const double *xi_x, *xi_y, *xi_z;
+} stz_cube_fields;
+
+int stz_mg_cube_values(const stz_cube_fields *f, int nx, int ny, int nz, int mode, float *out, void *stream);
+int stz_mg_output_cube(const stz_cube_fields *f, int nx, int ny, int nz, int mode, const char *dir,
+                       const char *prefix, int frame);
+
 #ifdef __cplusplus
 }
 #endif

@@ -108,20 +108,69 @@ def reference_available() -> bool:
     return os.path.exists(REF_LIB)
 
 
-def reference_step(fields, nx, ny, nz, prm, dt, lx=1.0, ly=1.0, lz=1.0, zper=False):
-    """One step of the unmodified reference on a copy of fields."""
+def _ref_lib():
     lib = ctypes.CDLL(REF_LIB)
     vp = ctypes.c_void_p
     lib.adv_new.restype = vp
-    lib.adv_new.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + [vp, ctypes.c_int]
+    lib.adv_new.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + [vp, ctypes.c_int, ctypes.c_char_p]
+    lib.adv_output_cube.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    return lib
+
+
+def _ref_params(prm):
+    return np.array([prm["mu"], prm["lamb"], prm["sy"], prm["tau0"], prm["c0"], prm["eps0"], prm["delta"],
+                     prm["omega"], prm["bath_temp"], prm["chi_inf"], prm["ez"], prm["diff_l"]])
+
+
+def reference_cube(fields, nx, ny, nz, prm, mode, outdir, prefix, frame):
+    """The unmodified reference's output_cube of Field member `mode` for the
+    Field array `fields`, appended to <outdir>/<prefix>_grid.<frame>."""
+    lib = _ref_lib()
+    vp = ctypes.c_void_p
+    p = _ref_params(prm)
+    h = lib.adv_new(nx, ny, nz, 1.0, 1.0, 1.0, p.ctypes.data_as(vp), 0, outdir.encode())
+    try:
+        buf = np.ascontiguousarray(fields, dtype=np.float64).copy()
+        lib.adv_set(h, buf.ctypes.data_as(vp))
+        lib.adv_output_cube(h, prefix.encode(), mode, frame)
+    finally:
+        lib.adv_free(h)
+
+
+def cube_values(fields, nx, ny, nz, mode):
+    """numpy restatement of output_cube's values (Field::fval, field.hh:157-177;
+    x slowest, z fastest; node-based members include the top z node), float32."""
+    g = NGHOST
+    zsize = nz + 1 if (mode <= 2 or mode >= 13) else nz
+    A = fields.reshape(nz + 2 * g, ny + 2 * g, nx + 2 * g, NFIELD)[g:g + zsize, g:g + ny, g:g + nx]
+    if mode in (9, 10):
+        s11, s22, s33 = A[..., S11], A[..., S22], A[..., S33]
+        p = -((s11 + s22) + s33) * (1 / 3.)
+        if mode == 9:
+            v = p
+        else:
+            t11, t22, t33 = s11 + p, s22 + p, s33 + p
+            q = 0.5 * ((t11 * t11 + t22 * t22) + t33 * t33)
+            q = ((q + A[..., S12] * A[..., S12]) + A[..., S13] * A[..., S13]) + A[..., S23] * A[..., S23]
+            v = np.sqrt(q)
+    elif mode == 12:
+        v = A[..., CHI] * 21000.
+    else:
+        v = A[..., {11: CHI, 13: 20, 14: 21, 15: 22}.get(mode, mode)]
+    return np.ascontiguousarray(v.transpose(2, 1, 0)).astype(np.float32).reshape(-1)
+
+
+def reference_step(fields, nx, ny, nz, prm, dt, lx=1.0, ly=1.0, lz=1.0, zper=False):
+    """One step of the unmodified reference on a copy of fields."""
+    lib = _ref_lib()
+    vp = ctypes.c_void_p
     lib.adv_npoints.argtypes = [vp]
     lib.adv_npoints.restype = ctypes.c_long
     lib.adv_set.argtypes = lib.adv_get.argtypes = [vp, vp]
     lib.adv_step.argtypes = [vp, ctypes.c_double]
     lib.adv_free.argtypes = [vp]
-    p = np.array([prm["mu"], prm["lamb"], prm["sy"], prm["tau0"], prm["c0"], prm["eps0"], prm["delta"],
-                  prm["omega"], prm["bath_temp"], prm["chi_inf"], prm["ez"], prm["diff_l"]])
-    h = lib.adv_new(nx, ny, nz, lx, ly, lz, p.ctypes.data_as(vp), int(zper))
+    p = _ref_params(prm)
+    h = lib.adv_new(nx, ny, nz, lx, ly, lz, p.ctypes.data_as(vp), int(zper), b"adv_harness_out")
     try:
         assert lib.adv_npoints(h) == fields.shape[0]
         buf = np.ascontiguousarray(fields, dtype=np.float64).copy()

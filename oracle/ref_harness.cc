@@ -434,4 +434,17 @@ int sr_solve(void *hp, double tol, int max_cycles, int bottom, int *cycles, doub
     GUARD_END
 }
 
+// region::output_x / output_r / output_residual of level l (region.cc:3062-3120):
+// the z-slice k written by output_internal (region.cc:3135-3202) to filename.
+// which: 0 x, 1 r, 2 residual.
+int sr_output_slice(void *hp, int l, int which, int k, double ax, double bx, double ay, double by,
+                    const char *filename) {
+    GUARD_BEGIN
+    region<vec3, mat3> *r = level((handle *)hp, l);
+    if (which == 0) r->output_x(ax, bx, ay, by, filename, k);
+    else if (which == 1) r->output_r(ax, bx, ay, by, filename, k);
+    else r->output_residual(ax, bx, ay, by, filename, k);
+    GUARD_END
+}
+
 }  // extern "C"

@@ -41,6 +41,8 @@ def _load():
     lib.sr_residual.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.sr_l2_error_all.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     lib.sr_solve.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.sr_output_slice.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
+        [ctypes.c_double] * 4 + [ctypes.c_char_p]
     _lib = lib
     return lib
 
@@ -115,6 +117,12 @@ class RefMultigrid:
     def set_field(self, l, which, v):
         v = np.ascontiguousarray(v, dtype=np.float64).reshape(self.npts(l), 3)
         self._check(_load().sr_set_field(self._h, l, {"x": 0, "r": 1}[which], _ptr(v)))
+
+    def output_slice(self, which, k, box, filename, l=0):
+        """region::output_x / output_r / output_residual (which: "x", "r",
+        "residual") of level l: z-slice k in box (ax, bx, ay, by) to filename."""
+        self._check(_load().sr_output_slice(self._h, l, {"x": 0, "r": 1, "residual": 2}[which], k, *box,
+                                            filename.encode()))
 
     def get_field(self, l, which):
         v = np.zeros((self.npts(l), 3))

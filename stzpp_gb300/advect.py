@@ -63,3 +63,42 @@ def advection_step(fields, dims, spacing, params, dt, work=None, stream=None, wa
                                    ctypes.byref(y) if wait else None)
     _mg._check(rc)
     return bool(y.value) if wait else None
+
+
+CUBE_MEMBERS = ("u", "v", "w", "s11", "s12", "s13", "s22", "s23", "s33", "chi", "xi_x", "xi_y", "xi_z")
+
+
+class CubeFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in CUBE_MEMBERS]
+
+
+def _cube_fields(fields):
+    return CubeFields(*[fields[k].data_ptr() if fields.get(k) is not None else None for k in CUBE_MEMBERS])
+
+
+def cube_values(fields, dims, mode, stream=None):
+    """shear_sim_3d::output_cube's values of Field member `mode` (0-15, as
+    Field::fval) on the device: a float32 CUDA tensor, x slowest, z fastest,
+    the node-based members with the top z node.  ``fields``: CUDA float64
+    tensors over the ghosted grid (members the mode does not read may be
+    missing)."""
+    import torch
+    nx, ny, nz = dims
+    zsize = nz + 1 if (mode <= 2 or mode >= 13) else nz
+    out = torch.empty(nx * ny * zsize, dtype=torch.float32, device=next(iter(fields.values())).device)
+    f = _cube_fields(fields)
+    st = (stream or torch.cuda.current_stream()).cuda_stream
+    _mg._check(_mg.load_library().stz_mg_cube_values(ctypes.byref(f), nx, ny, nz, mode,
+                                                     ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(st)))
+    return out
+
+
+def output_cube(fields, dims, mode, directory, prefix, frame):
+    """Append Field member `mode` to <directory>/<prefix>_grid.<frame> in the
+    reference's cube format (shear_sim_3d::output_cube)."""
+    import os
+    import torch
+    torch.cuda.current_stream().synchronize()
+    f = _cube_fields(fields)
+    _mg._check(_mg.load_library().stz_mg_output_cube(ctypes.byref(f), *dims, mode, os.fsencode(directory),
+                                                     prefix.encode(), frame))

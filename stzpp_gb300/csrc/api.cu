@@ -1375,6 +1375,36 @@ int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq
 }
 
 
+int stz_mg_output_slice(stz_mg_handle h, int which, int k, double ax, double bx, double ay, double by,
+                        const char *filename) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        if (which < STZ_MG_SLICE_X || which > STZ_MG_SLICE_RESIDUAL || !filename)
+            fail(STZ_MG_ERR_ARG, "stz_mg_output_slice: which must be STZ_MG_SLICE_X, _R or _RESIDUAL");
+        const Geom &g = h->geo[0];
+        if (k < 0 || k >= g.o) fail(STZ_MG_ERR_ARG, "stz_mg_output_slice: slice out of range");
+        if (g.m < 2 || g.n < 2) fail(STZ_MG_ERR_ARG, "stz_mg_output_slice: needs m, n >= 2");
+        const double *f = h->L64[0].x;
+        if (which == STZ_MG_SLICE_R) f = h->L64[0].r;
+        if (which == STZ_MG_SLICE_RESIDUAL) {
+            need_setup(h);
+            launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L64[0].res, nullptr,
+                                            nullptr, h->st);
+            check_launch();
+            f = h->L64[0].res;
+        }
+        const size_t n = (size_t)g.m * g.n;
+        float *d = reinterpret_cast<float *>(staging(h, (n + 1) / 2));
+        launch_slice(g, f, k, which == STZ_MG_SLICE_RESIDUAL, d, h->st);
+        check_launch();
+        std::vector<float> vals(n);
+        CK(cudaMemcpyAsync(vals.data(), d, n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        if (!write_slice_file(vals.data(), g.m, g.n, ax, bx, ay, by, filename))
+            fail(STZ_MG_ERR_ARG, "stz_mg_output_slice: cannot write %s", filename);
+    });
+}
+
 int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
                        double *work_per_launch) {
     if (!h || reps < 1) return set_error(STZ_MG_ERR_ARG, "bad argument");

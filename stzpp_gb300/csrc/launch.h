@@ -43,6 +43,12 @@ int residual_tile_blocks(const Geom &g, bool fp64);
 template <typename T>
 void launch_residual_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, double *partial,
                           cudaStream_t st);
+// output.cu: a z-slice of a top-level vec3 field (colour-blocked) as floats
+// of |v|^2 (|v|^2 |v|^2 with quartic), m x n natural order; the file of
+// region::output_internal for one process
+void launch_slice(const Geom &g, const double *f, int k, bool quartic, float *out, cudaStream_t st);
+bool write_slice_file(const float *vals, int m, int n, double ax, double bx, double ay, double by,
+                      const char *filename);
 int residual_blocks(const Geom &g);
 // res = r - A x (res may be null); when partial is non-null, per-block sums of
 // |res|^2 go to partial[residual_blocks(g)] and, when out is non-null, their

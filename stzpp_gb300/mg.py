@@ -41,6 +41,7 @@ EXPORTS = (
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
     "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
     "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update", "stz_mg_advection_step",
+    "stz_mg_output_slice", "stz_mg_cube_values", "stz_mg_output_cube",
 )
 
 # measurement hook kernel ids (include/stz_mg.h)
@@ -105,6 +106,9 @@ def load_library():
     lib.stz_mg_coeff_grad.argtypes = [vp, vp, vp, vp, vp, ci]
     lib.stz_mg_stress_update.argtypes = [vp, vp, cd, cd, cd, cd, cd, cd, ctypes.POINTER(cd), ci]
     lib.stz_mg_advection_step.argtypes = [vp, vp, cd, vp, ctypes.POINTER(ci)]
+    lib.stz_mg_output_slice.argtypes = [vp, ci, ci, cd, cd, cd, cd, ctypes.c_char_p]
+    lib.stz_mg_cube_values.argtypes = [vp, ci, ci, ci, ci, vp, vp]
+    lib.stz_mg_output_cube.argtypes = [vp, ci, ci, ci, ci, ctypes.c_char_p, ctypes.c_char_p, ci]
     for name in EXPORTS:
         if name not in ("stz_mg_desc_default", "stz_mg_last_error"):
             getattr(lib, name).restype = ci
@@ -427,6 +431,16 @@ class Multigrid:
         _check(load_library().stz_mg_level_residual(self._h, l, out.ctypes.data_as(ctypes.c_void_p),
                                                     ctypes.byref(sq), HOST))
         return out, sq.value
+
+    def output_slice(self, which, k, filename, box=None):
+        """region::output_x / output_r / output_residual: the z-slice k of the
+        solution ("x"), right-hand side ("r") or residual ("residual") written
+        to filename in the reference's slice format; box = (ax, bx, ay, by),
+        default (0, m-1, 0, n-1)."""
+        m, n, _ = self.dims
+        ax, bx, ay, by = box if box is not None else (0.0, m - 1.0, 0.0, n - 1.0)
+        code = {"x": 0, "r": 1, "residual": 2}[which]
+        _check(load_library().stz_mg_output_slice(self._h, code, k, ax, bx, ay, by, os.fsencode(filename)))
 
     def time_kernel(self, kernel, level=0, reps=20):
         """(ms per launch, algorithmic bytes or FP64 flops per launch) of one

@@ -28,7 +28,12 @@ Also ``adv``: the reference's quasi-static advection step
 (``make -C oracle advref``) on seeded ghosted grids -> tests/golden/adv_step.npz
 (inputs and the changed Field members of every point).
 
-Run: python tests/golden/make_golden.py [trans | adv]
+Also ``out``: the files the reference's own writers produce -- every
+Field member of shear_sim_3d::output_cube on a seeded 6x5x4 grid, and the
+x, r and residual z-slices of region::output_internal on an 8x6x5 multigrid
+level -> tests/golden/output_files.npz (inputs and file bytes).
+
+Run: python tests/golden/make_golden.py [trans | adv | out]
 """
 import os
 import sys
@@ -139,7 +144,48 @@ def adv_steps(path):
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+OUT_CUBE = (6, 5, 4)
+OUT_SLICE = ((8, 6, 5), (True, True, False), 2, [(0.0, 7.0, 0.0, 5.0), (0.0, 1.0, -0.5, 0.5)])
+OUT_COLS = list(range(10)) + [20, 21, 22]   # u v w s11..s33 chi xi_x xi_y xi_z
+
+
+def output_files(path):
+    import tempfile
+    from oracle import advect as A
+    if not (A.reference_available() and refpy.available()):
+        sys.exit("oracle/_ref/libstzadv.so and libstzref.so are needed: `make -C oracle ref advref`")
+    out = {}
+    d = tempfile.mkdtemp()
+    nx, ny, nz = OUT_CUBE
+    F = A.random_fields(21, nx, ny, nz, plastic_bias=0.5)
+    F[:, 20:23] = np.random.default_rng(22).normal(size=(F.shape[0], 3))
+    out["cube/in"] = F[:, OUT_COLS]
+    for mode in range(16):
+        A.reference_cube(F, nx, ny, nz, A.driver_params(nx), mode, os.path.join(d, "cube"), f"m{mode}", 3)
+        out[f"cube/{mode}"] = np.frombuffer(open(os.path.join(d, "cube", f"m{mode}_grid.3"), "rb").read(), np.uint8)
+    dims, per, k, boxes = OUT_SLICE
+    st, fix = P.elastic_stencil_const(1.0, 2.0, 1 / dims[0], 1 / dims[1], 1 / (dims[2] - 1))
+    R = refpy.RefMultigrid(dims, per, stencil=st, fix=fix, max_coarse=16)
+    rng = np.random.default_rng(23)
+    x, r = rng.normal(size=(int(np.prod(dims)), 3)), rng.normal(size=(int(np.prod(dims)), 3))
+    R.set_field(0, "x", x)
+    R.set_field(0, "r", r)
+    out["slice/x"], out["slice/r"] = x, r
+    for which in ("x", "r", "residual"):
+        for b, box in enumerate(boxes):
+            fn = os.path.join(d, f"{which}{b}")
+            R.residual(0)   # the periodic ghosts output_residual reads
+            R.output_slice(which, k, box, fn)
+            out[f"slice/{which}/{b}"] = np.frombuffer(open(fn, "rb").read(), np.uint8)
+    R.close()
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "out":
+        output_files(os.path.join(HERE, "output_files.npz"))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "adv":
         adv_steps(os.path.join(HERE, "adv_step.npz"))
         return
