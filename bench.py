@@ -228,7 +228,7 @@ def run_ours(args, world, rank, local):
         return reduce_max(v, dist, "cuda" if dist is None or dist.get_backend() == "nccl" else "cpu")
 
     # ---------------------------------------------------------- mixed solve
-    mg = sg.Multigrid(dims, per, precision="mixed", v_down=V_DOWN, v_up=V_UP, sweep_growth=False,
+    mg = sg.Multigrid(dims, per, precision="mixed", v_down=args.v_down, v_up=args.v_up, sweep_growth=False,
                       max_coarse=args.max_coarse, device=local, stream=stream.cuda_stream)
     t0 = time.perf_counter()
     mg.setup_matrices(stencil=stencil, fix=fix)
@@ -675,6 +675,8 @@ def main():
                          "5: 50-solve sequence with checkpointed backward; 6: per-step coefficient change; "
                          "7: the quasi-static advection step on 256^3 cells")
     ap.add_argument("--cells", type=int, default=256, help="cells per dimension of the advection workload (--config 7)")
+    ap.add_argument("--v-down", type=int, default=V_DOWN, help="sweeps before the coarse-grid correction")
+    ap.add_argument("--v-up", type=int, default=V_UP, help="sweeps after it")
     ap.add_argument("--max-coarse", type=int, default=1024,
                     help="hierarchy stop rule of the headline solve (reference: 1024 nodes)")
     args = ap.parse_args()
