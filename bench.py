@@ -228,8 +228,9 @@ def run_ours(args, world, rank, local):
         return reduce_max(v, dist, "cuda" if dist is None or dist.get_backend() == "nccl" else "cpu")
 
     # ---------------------------------------------------------- mixed solve
-    mg = sg.Multigrid(dims, per, precision="mixed", v_down=args.v_down, v_up=args.v_up, sweep_growth=False,
-                      max_coarse=args.max_coarse, device=local, stream=stream.cuda_stream)
+    mg = sg.Multigrid(dims, per, precision="mixed", v_down=args.v_down, v_up=args.v_up,
+                      sweep_growth=bool(args.sweep_growth), max_coarse=args.max_coarse, device=local,
+                      stream=stream.cuda_stream)
     t0 = time.perf_counter()
     mg.setup_matrices(stencil=stencil, fix=fix)
     torch.cuda.synchronize()
@@ -677,6 +678,8 @@ def main():
     ap.add_argument("--cells", type=int, default=256, help="cells per dimension of the advection workload (--config 7)")
     ap.add_argument("--v-down", type=int, default=V_DOWN, help="sweeps before the coarse-grid correction")
     ap.add_argument("--v-up", type=int, default=V_UP, help="sweeps after it")
+    ap.add_argument("--sweep-growth", type=int, choices=[0, 1], default=0,
+                    help="1: v_down + i / v_up + i - 1 sweeps on level i, as the reference")
     ap.add_argument("--max-coarse", type=int, default=1024,
                     help="hierarchy stop rule of the headline solve (reference: 1024 nodes)")
     args = ap.parse_args()
