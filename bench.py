@@ -47,8 +47,11 @@ WORKLOAD = ("quasi-static projection solve, 256x256x257 nodes (257^3 problem: pe
             "to relative residual 1e-10")
 CPU_SAMPLE_DIMS = (64, 64, 65)
 # Cycle of the GPU solves: two sweeps down, three up on every level.  Measured
-# at 256x256x257 on a GB300 (mixed / FP64 ms per solve): V(2,2) 44.2 / 242,
-# V(2,3) 41.8 / 222, V(3,3) 43.5 / 231, V(3,2) 45.1 / 222, V(2,1) 53.9 / 260.
+# at 256x256x257 on a GB300 (mixed / FP64 ms per solve, earlier kernels):
+# V(2,2) 44.2 / 242, V(2,3) 41.8 / 222, V(3,3) 43.5 / 231, V(3,2) 45.1 / 222,
+# V(2,1) 53.9 / 260; with the current kernels V(2,3) 36.7 ms (11 cycles)
+# against the reference's growing schedule (v + i sweeps on level i):
+# V(1,2) 57.2 (20 cycles), V(2,2) 46.0 (14), V(1,3) 46.5 (14), V(1,1) 68.7 (30).
 V_DOWN, V_UP = 2, 3
 
 
