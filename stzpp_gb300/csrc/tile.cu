@@ -500,16 +500,25 @@ __global__ void __launch_bounds__(kTileThreads, kMarchMinBlocks<T>)
     }
 }
 
+// The shared-memory attribute of a kernel is set per device: true the first
+// time this is asked on the current device (setting it twice is harmless).
+bool first_use_on_device(unsigned long long &devices) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (devices & bit) return false;
+    devices |= bit;
+    return true;
+}
+
 template <typename T, int KIND, bool ELASTIC, bool SPARSE>
 void launch_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     const int tiles = (g.m / kTX) * (g.n / kTY);
     auto kern = gs_tile_kernel<T, KIND, ELASTIC, SPARSE>;
     const int smem = (int)sizeof(TileBuf<T>);
-    static bool attr_set = false;   // per instantiation
-    if (!attr_set) {
+    static unsigned long long attr_devices = 0;   // per instantiation
+    if (first_use_on_device(attr_devices))
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set = true;
-    }
     for (int c = 0; c < 2; c++) {
         const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
         if (planes > 0) kern<<<dim3(tiles, planes), kGsThreads, smem, st>>>(g, c, op, r, xin, xout);
@@ -539,13 +548,12 @@ void launch_res_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T 
     const int smem = kMarchSmemWords * (int)sizeof(T);
     const int zlen = march_zlen<T>(g);
     const dim3 grid((g.m / kTX) * (g.n / kTY), (g.o + zlen - 1) / zlen);
-    static bool attr_set = false;   // per instantiation
-    if (!attr_set) {
+    static unsigned long long attr_devices = 0;   // per instantiation
+    if (first_use_on_device(attr_devices)) {
         cudaFuncSetAttribute(residual_tile_kernel<T, KIND, ELASTIC, SPARSE, false>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaFuncSetAttribute(residual_tile_kernel<T, KIND, ELASTIC, SPARSE, true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        attr_set = true;
     }
     if (partial)
         residual_tile_kernel<T, KIND, ELASTIC, SPARSE, true>
