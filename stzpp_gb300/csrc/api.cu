@@ -126,7 +126,8 @@ struct stz_mg_handle_s {
     template <typename T>
     T *alloc(size_t n) {
         void *p = nullptr;
-        CK(cudaMalloc(&p, n * sizeof(T) ? n * sizeof(T) : 1));
+        const size_t bytes = n * sizeof(T);
+        CK(cudaMalloc(&p, bytes ? bytes : 1));
         allocs.push_back(p);
         return (T *)p;
     }

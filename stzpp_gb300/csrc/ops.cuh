@@ -213,7 +213,7 @@ __host__ __device__ constexpr bool coarse_entry(int b, int e) {
 template <typename T, bool SPARSE, bool WITH_CENTRE, bool COH = false>
 __device__ inline void plane_row_coef(const T *cf, int stride, const Geom &g, const NbrOffsets &t,
                                       const T *__restrict__ x, T *acc) {
-    if (sizeof(T) == 8) {
+    if constexpr (sizeof(T) == 8) {
         // FP64: arithmetic bound; load each neighbour right before its block
 #pragma unroll
         for (int b = 0; b < 27; b++) {
@@ -226,25 +226,25 @@ __device__ inline void plane_row_coef(const T *cf, int stride, const Geom &g, co
             for (int e = 0; e < 9; e++)
                 if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[(9 * b + e) * stride] * v[e % 3];
         }
-        return;
-    }
-    // FP32: all neighbour loads are issued before the arithmetic so that they
-    // are in flight together (one memory latency per node, not one per block)
-    T v[27][3];
+    } else {
+        // FP32: all neighbour loads are issued before the arithmetic so that
+        // they are in flight together (one memory latency per node, not one per block)
+        T v[27][3];
 #pragma unroll
-    for (int b = 0; b < 27; b++) {
-        if (b == 13 && !WITH_CENTRE) continue;
-        int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
-        const int sc = s < 0 ? 0 : s;
-        load3<T, COH>(x, g.npad, sc, v[b]);
-        if (s < 0) v[b][0] = v[b][1] = v[b][2] = T(0);
-    }
+        for (int b = 0; b < 27; b++) {
+            if (b == 13 && !WITH_CENTRE) continue;
+            int s = t.ox[bdx(b) + 1] + t.oy[bdy(b) + 1] + t.oz[bdz(b) + 1];
+            const int sc = s < 0 ? 0 : s;
+            load3<T, COH>(x, g.npad, sc, v[b]);
+            if (s < 0) v[b][0] = v[b][1] = v[b][2] = T(0);
+        }
 #pragma unroll
-    for (int b = 0; b < 27; b++) {
-        if (b == 13 && !WITH_CENTRE) continue;
+        for (int b = 0; b < 27; b++) {
+            if (b == 13 && !WITH_CENTRE) continue;
 #pragma unroll
-        for (int e = 0; e < 9; e++)
-            if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[(9 * b + e) * stride] * v[b][e % 3];
+            for (int e = 0; e < 9; e++)
+                if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[(9 * b + e) * stride] * v[b][e % 3];
+        }
     }
 }
 
