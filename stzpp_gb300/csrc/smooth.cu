@@ -23,10 +23,10 @@ constexpr int kBlock = 256;
 
 // Colour kernels run on a 3-D grid: block (32, 8), grid (ceil(M2/32),
 // ceil(N2/8), number of sub-grid planes); thread -> sub-grid coordinates
-// (I, J, K) of colour q, K = k0 + blockIdx.z.
+// (I, J, K) of colour q; the sub-grid planes K in reverse order when rev.
 #define COLOUR_NODE_PROLOGUE                                                                    \
     const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y; \
-    const int K = k0 + (int)blockIdx.z;                                                         \
+    const int K = rev ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;                     \
     if (I >= g.M2 || J >= g.N2) return;                                                         \
     const int i = 2 * I + (q & 1), j = 2 * J + ((q >> 1) & 1), k = 2 * K + (q >> 2);             \
     if (i >= g.m || j >= g.n || k >= g.o) return;                                               \
@@ -34,7 +34,7 @@ constexpr int kBlock = 256;
 
 // ------------------------------------------------------------------ GS
 template <typename T, bool ELASTIC>
-__global__ void __launch_bounds__(kBlock) gs_const_kernel(Geom g, int q, int k0, const __grid_constant__ ConstOp<T> op,
+__global__ void __launch_bounds__(kBlock) gs_const_kernel(Geom g, int q, int rev, const __grid_constant__ ConstOp<T> op,
                                                           const T *__restrict__ r, T *__restrict__ x) {
     COLOUR_NODE_PROLOGUE
     T acc[3];
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kBlock) gs_const_kernel(Geom g, int q, int k0,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) gs_lame_kernel(Geom g, int q, int k0, LameOp<T> op, const T *__restrict__ r,
+__global__ void __launch_bounds__(kBlock) gs_lame_kernel(Geom g, int q, int rev, LameOp<T> op, const T *__restrict__ r,
                                                          T *__restrict__ x) {
     COLOUR_NODE_PROLOGUE
     T acc[3];
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kBlock) gs_lame_kernel(Geom g, int q, int k0, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) gs_dense_kernel(Geom g, int q, int k0, DenseOp<T> op, const T *__restrict__ r,
+__global__ void __launch_bounds__(kBlock) gs_dense_kernel(Geom g, int q, int rev, DenseOp<T> op, const T *__restrict__ r,
                                                           T *__restrict__ x) {
     COLOUR_NODE_PROLOGUE
     T acc[3];
@@ -94,11 +94,11 @@ __global__ void __launch_bounds__(kBlock) gs_dense_kernel(Geom g, int q, int k0,
 // plane, so the row of that plane (243 block entries and the 9 entries of the
 // inverse centre block) is staged in shared memory once per block.
 template <typename T, bool SPARSE>
-__global__ void __launch_bounds__(kBlock) gs_plane_kernel(Geom g, int q, int k0, PlaneOp<T> op, const T *__restrict__ r,
+__global__ void __launch_bounds__(kBlock) gs_plane_kernel(Geom g, int q, int rev, PlaneOp<T> op, const T *__restrict__ r,
                                                           T *__restrict__ x) {
     __shared__ T cf[252];
     {
-        const int k = 2 * (k0 + (int)blockIdx.z) + (q >> 2);
+        const int k = 2 * (rev ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z) + (q >> 2);
         for (int e = threadIdx.y * blockDim.x + threadIdx.x; e < 252; e += blockDim.x * blockDim.y)
             cf[e] = k < g.o ? (e < 243 ? op.coef[e * op.O + k] : op.dinv[(e - 243) * op.O + k]) : T(0);
         __syncthreads();
@@ -290,29 +290,32 @@ __global__ void sum_partials_kernel(const double *__restrict__ partial, int n, d
 }
 
 // ------------------------------------------------------------- launchers
-// Colour q on the sub-grid planes K in [k0, k0 + nk).
+// Colour q on every sub-grid plane, taken in reverse order when rev.
 template <typename T>
-static void launch_gs_colour_planes(const LevelOp<T> &op, const Geom &g, int q, int k0, int nk, const T *r, T *x,
+static void launch_gs_colour_planes(const LevelOp<T> &op, const Geom &g, int q, int rev, const T *r, T *x,
                                     cudaStream_t st) {
-    if (nk <= 0) return;
-    const dim3 blocks((g.M2 + 31) / 32, (g.N2 + 7) / 8, nk), blk(32, 8);
+    const dim3 blocks((g.M2 + 31) / 32, (g.N2 + 7) / 8, g.O2), blk(32, 8);
     switch (op.kind) {
         case OP_CONST:
-            if (op.cop.elastic) gs_const_kernel<T, true><<<blocks, blk, 0, st>>>(g, q, k0, op.cop, r, x);
-            else gs_const_kernel<T, false><<<blocks, blk, 0, st>>>(g, q, k0, op.cop, r, x);
+            if (op.cop.elastic) gs_const_kernel<T, true><<<blocks, blk, 0, st>>>(g, q, rev, op.cop, r, x);
+            else gs_const_kernel<T, false><<<blocks, blk, 0, st>>>(g, q, rev, op.cop, r, x);
             break;
-        case OP_LAME: gs_lame_kernel<T><<<blocks, blk, 0, st>>>(g, q, k0, op.lop, r, x); break;
+        case OP_LAME: gs_lame_kernel<T><<<blocks, blk, 0, st>>>(g, q, rev, op.lop, r, x); break;
         case OP_PLANE:
-            if (op.pop.sparse) gs_plane_kernel<T, true><<<blocks, blk, 0, st>>>(g, q, k0, op.pop, r, x);
-            else gs_plane_kernel<T, false><<<blocks, blk, 0, st>>>(g, q, k0, op.pop, r, x);
+            if (op.pop.sparse) gs_plane_kernel<T, true><<<blocks, blk, 0, st>>>(g, q, rev, op.pop, r, x);
+            else gs_plane_kernel<T, false><<<blocks, blk, 0, st>>>(g, q, rev, op.pop, r, x);
             break;
-        default: gs_dense_kernel<T><<<blocks, blk, 0, st>>>(g, q, k0, op.dop, r, x); break;
+        default: gs_dense_kernel<T><<<blocks, blk, 0, st>>>(g, q, rev, op.dop, r, x); break;
     }
 }
 
 template <typename T>
 void launch_gs_colour(const LevelOp<T> &op, const Geom &g, int q, const T *r, T *x, cudaStream_t st) {
-    launch_gs_colour_planes(op, g, q, 0, g.O2, r, x, st);
+    // Odd colours walk the planes downwards ("snake" order): a colour pass
+    // starts where the previous one ended, on neighbour sub-grids still in L2.
+    // Updates within one colour are independent, so the order changes no bit.
+    // Fine FP32 level, 256x256x257, two sweeps: 658 -> 614 us.
+    launch_gs_colour_planes(op, g, q, q & 1, r, x, st);
 }
 
 // Large planes: one launch per colour keeps millions of threads in flight;
