@@ -730,19 +730,34 @@ void run_vcycle32(stz_mg_handle h, int count) {
 
 // |b - A x|^2 of the top FP64 level; when r32 is non-null the residual is
 // also written there in FP32 (the right-hand side of the correction solve).
+double rhs_norm(stz_mg_handle h);
+
+// The residual of the mixed solver's correction steps (r32 non-null): in
+// double-float arithmetic on a shared-stencil top level (residual_df.cu),
+// with x split into the FP32 level's x and res fields -- both free between
+// correction solves -- else in FP64.  Returns |b - A x|^2 in FP64.
 double top_residual_sq(stz_mg_handle h, float *r32) {
     const Geom &g = h->geo[0];
-    if (r32)
+    double unscale = 1.0;
+    if (r32 && residual_df_applies(h->op64[0])) {
+        const double bn = rhs_norm(h);
+        const double scale = df_norm_scale(bn * bn, 3 * npts(g));
+        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].x, h->L32[0].res, r32, scale,
+                           h->partial, h->dscal, h->st);
+        unscale = 1.0 / (scale * scale);
+        h->stat_launches += 1;   // the split of x
+    } else if (r32) {
         launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, r32, h->partial, h->dscal, h->st);
-    else
+    } else {
         launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial,
                                         h->dscal, h->st);
+    }
     check_launch();
     h->stat_residuals++;
     h->stat_launches += 2;   // residual + partial-sum reduction
     CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     sync(h);
-    double v = h->hscal[0];
+    double v = h->hscal[0] * unscale;
     if (!std::isfinite(v)) fail(STZ_MG_ERR_NONFINITE, "residual is not finite");
     return v;
 }
@@ -1466,7 +1481,14 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
                 const LevelOp<double> &op = h->op64[0];
                 double fma = op.kind == OP_CONST && op.cop.elastic ? 51 : op.kind == OP_LAME ? 51 : 243;
                 work = 2 * fma * npts_l;
-                if (mixed) launch = [&] { launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].r, h->partial, h->dscal, h->st); };
+                if (mixed && residual_df_applies(op)) {
+                    // the mixed solver's pass: split of x + double-float residual + sum
+                    const double scale = df_norm_scale(rhs_norm(h) * rhs_norm(h), 3 * npts(g));
+                    launch = [&, scale] {
+                        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].x, h->L32[0].res,
+                                           h->L32[0].r, scale, h->partial, h->dscal, h->st);
+                    };
+                } else if (mixed) launch = [&] { launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].r, h->partial, h->dscal, h->st); };
                 else launch = [&] { launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial, h->dscal, h->st); };
                 break;
             }

@@ -289,6 +289,10 @@ __global__ void sum_partials_kernel(const double *__restrict__ partial, int n, d
     }
 }
 
+void launch_sum_partials(const double *partial, int n, double *out, cudaStream_t st) {
+    sum_partials_kernel<<<1, 1024, 0, st>>>(partial, n, out);
+}
+
 // ------------------------------------------------------------- launchers
 // Colour q on every sub-grid plane, taken in reverse order when rev.
 template <typename T>

@@ -176,6 +176,41 @@ def test_solution_matches_reference_solver(precision, kind, oracle_port):
     assert err <= SOLUTION_RTOL, f"{precision}/{kind}: {cycles} cycles, error {err:.3e}"
 
 
+@pytest.mark.parametrize("kind", ["const", "trans"])
+def test_double_float_residual_matches_fp64(kind, monkeypatch):
+    """The mixed solver's top-level residual in double-float arithmetic (FP32
+    pairs, exact products, compensated sums): after 3, 6, 9 and 12 cycles the
+    relative residual it reports equals the FP64 residual norm of the same x
+    to 1e-3 of itself plus 1e-13, and a solve with the FP64 residual kernel
+    (STZ_MG_DF=0) takes the same number of cycles to a solution within 1e-10
+    of it (both stop at a relative residual near 1e-10).  64x64x65, dx = 1/64, the elastic and a full non-symmetric shared
+    stencil."""
+    import stzpp_gb300 as sg
+    dims, per = (64, 64, 65), (True, True, False)
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, dx, dy, dz)
+    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz) if kind == "const" else trans_stencil(2, dx)
+    for cap in (3, 6, 9, 12):
+        with sg.Multigrid(dims, per, precision="mixed") as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            mg.setup_fields(r=b)
+            cycles, rel = mg.solve(1e-14, cap, check=False)
+            rn, bn = mg.residual_norm()
+        assert cycles == cap
+        assert abs(rel - rn / bn) <= 1e-3 * (rn / bn) + 1e-13, f"{cap} cycles: {rel:.6e} vs FP64 {rn / bn:.6e}"
+    out = {}
+    for df in ("1", "0"):
+        monkeypatch.setenv("STZ_MG_DF", df)
+        with sg.Multigrid(dims, per, precision="mixed") as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            mg.setup_fields(r=b)
+            out[df] = mg.solve(1e-10, 100) + (mg.get_x(),)
+    assert out["1"][0] == out["0"][0]
+    assert out["1"][1] <= 1e-10 and out["0"][1] <= 1e-10
+    assert np.linalg.norm(out["1"][2] - out["0"][2]) <= 1e-10 * np.linalg.norm(out["0"][2])
+
+
 def test_reference_hierarchy_gs_bottom(oracle_port):
     """The reference's own cycle shape (coarsest <= 1024 nodes, 24 GS sweeps)."""
     mg, ref = build_pair((32, 32, 33), (True, True, False), "const", oracle_port, max_coarse=1024, bottom="gs")
