@@ -734,16 +734,17 @@ double rhs_norm(stz_mg_handle h);
 
 // The residual of the mixed solver's correction steps (r32 non-null): in
 // double-float arithmetic on a shared-stencil top level (residual_df.cu),
-// with x split into the FP32 level's x and res fields -- both free between
-// correction solves -- else in FP64.  Returns |b - A x|^2 in FP64.
+// with x split into float pairs in the FP64 level's res field (scratch: the
+// calls that report a residual recompute it there) -- else in FP64.
+// Returns |b - A x|^2 in FP64.
 double top_residual_sq(stz_mg_handle h, float *r32) {
     const Geom &g = h->geo[0];
     double unscale = 1.0;
     if (r32 && residual_df_applies(h->op64[0])) {
         const double bn = rhs_norm(h);
         const double scale = df_norm_scale(bn * bn, 3 * npts(g));
-        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].x, h->L32[0].res, r32, scale,
-                           h->partial, h->dscal, h->st);
+        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, reinterpret_cast<float2 *>(h->L64[0].res), r32,
+                           scale, h->partial, h->dscal, h->st);
         unscale = 1.0 / (scale * scale);
         h->stat_launches += 1;   // the split of x
     } else if (r32) {
@@ -1485,8 +1486,9 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
                     // the mixed solver's pass: split of x + double-float residual + sum
                     const double scale = df_norm_scale(rhs_norm(h) * rhs_norm(h), 3 * npts(g));
                     launch = [&, scale] {
-                        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].x, h->L32[0].res,
-                                           h->L32[0].r, scale, h->partial, h->dscal, h->st);
+                        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x,
+                                           reinterpret_cast<float2 *>(h->L64[0].res), h->L32[0].r, scale, h->partial,
+                                           h->dscal, h->st);
                     };
                 } else if (mixed) launch = [&] { launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L32[0].r, h->partial, h->dscal, h->st); };
                 else launch = [&] { launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, (double *)nullptr, h->partial, h->dscal, h->st); };

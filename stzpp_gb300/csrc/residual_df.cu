@@ -7,12 +7,14 @@
 // on the 256x256x257 problem, 12 % of the solve.  Here every FP64 value is
 // carried as a pair of floats (hi + lo, about 47 significant bits):
 //
-//  * x is split once per residual into two float fields (split_kernel), b
-//    per node as it is read, the shared stencil on the host;
+//  * x is split once per residual into float pairs (split_kernel; one 8-byte
+//    load per neighbour component), b per node as it is read, the shared
+//    stencil on the host;
 //  * a product a x = (ah + al)(xh + xl) is ah*xh exactly -- its rounded value
 //    p and its error fma(ah, xh, -p) (Dekker, "A floating-point technique for
 //    extending the available precision", 1971) -- plus the two cross terms
-//    ah*xl + al*xh (the al*xl term, 2^-48 of the product, is dropped);
+//    ah*xl + al*xh (the al*xl term, 2^-48 of the product, is dropped; a
+//    stencil exact in FP32 has al = 0 and a kernel without the al terms);
 //  * the running sum keeps its high part exact with Knuth's two-sum (The Art
 //    of Computer Programming vol. 2, 4.2.2) and gathers every rounding error
 //    and small term in a float low part.
@@ -96,7 +98,8 @@ __host__ __device__ inline void split_double(double x, float &hi, float &lo) {
     lo = sign ? -v : v;
 }
 
-// (sh, sl) -= (ah + al)(xh + xl)
+// (sh, sl) -= (ah + al)(xh + xl); AL false: al is 0
+template <bool AL>
 __device__ __forceinline__ void df_sub_prod(float &sh, float &sl, float ah, float al, float xh, float xl) {
     const float p = __fmul_rn(ah, xh);
     const float ep = __fmaf_rn(ah, xh, -p);   // ah*xh = p + ep exactly
@@ -104,28 +107,28 @@ __device__ __forceinline__ void df_sub_prod(float &sh, float &sl, float ah, floa
     const float bv = __fsub_rn(s, sh);
     const float err = __fsub_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fadd_rn(p, bv));
     sh = s;
-    const float cross = __fmaf_rn(ah, xl, __fmul_rn(al, xh));
+    const float cross = AL ? __fmaf_rn(ah, xl, __fmul_rn(al, xh)) : __fmul_rn(ah, xl);
     sl = __fsub_rn(__fadd_rn(sl, __fsub_rn(err, ep)), cross);
 }
 
-__global__ void split_kernel(const double *__restrict__ x, float *__restrict__ hi, float *__restrict__ lo, size_t n) {
+__global__ void split_kernel(const double *__restrict__ x, float2 *__restrict__ xs, size_t n) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-        float h, l;
-        split_double(x[t], h, l);
-        hi[t] = h;
-        lo[t] = l;
+        float2 v;
+        split_double(x[t], v.x, v.y);
+        xs[t] = v;
     }
 }
 
 // r32 = b - A x over every slot of the top level (unused slots get 0) and,
-// per block, the FP64 sum of (scale * r32)^2 into partial.  Thread layout of
-// residual_kernel: block (32, 8), lanes along x, threadIdx.y the colour.
-template <bool ELASTIC>
+// per block, the FP64 sum of (scale * r32)^2 into partial; xs: x as
+// (hi, lo) pairs.  Thread layout of residual_kernel: block (32, 8), lanes
+// along x, threadIdx.y the colour.
+template <bool ELASTIC, bool AL>
 __global__ void __launch_bounds__(kDfThreads) residual_df_kernel(Geom g, const __grid_constant__ DfConst op,
                                                                  int centre_diag, const double *__restrict__ b,
-                                                                 const float *__restrict__ xh,
-                                                                 const float *__restrict__ xl, float *__restrict__ r32,
-                                                                 float scale, double *__restrict__ partial) {
+                                                                 const float2 *__restrict__ xs,
+                                                                 float *__restrict__ r32, float scale,
+                                                                 double *__restrict__ partial) {
     const int q = threadIdx.y;
     const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y, K = blockIdx.z;
     const int a = q & 1, bq = (q >> 1) & 1, c = q >> 2;
@@ -151,26 +154,29 @@ __global__ void __launch_bounds__(kDfThreads) residual_df_kernel(Geom g, const _
                         bool used = !ELASTIC || blk == 13;
 #pragma unroll
                         for (int rr = 0; rr < 3; rr++) used = used || elastic_entry(blk, 3 * rr + cc);
-                        vh[cc] = used ? xh[s + cc * np] : 0.0f;
-                        vl[cc] = used ? xl[s + cc * np] : 0.0f;
+                        const float2 v = used ? xs[s + cc * np] : make_float2(0.0f, 0.0f);
+                        vh[cc] = v.x;
+                        vl[cc] = v.y;
                     }
 #pragma unroll
                     for (int e = 0; e < 9; e++) {
                         if (ELASTIC && blk != 13 && !elastic_entry(blk, e)) continue;
                         if (blk == 13 && centre_diag && e % 4 != 0) continue;   // warp-uniform
                         if (!ELASTIC && op.ah[blk][e] == 0.0f) continue;      // warp-uniform
-                        df_sub_prod(sh[e / 3], sl[e / 3], op.ah[blk][e], op.al[blk][e], vh[e % 3], vl[e % 3]);
+                        df_sub_prod<AL>(sh[e / 3], sl[e / 3], op.ah[blk][e], op.al[blk][e], vh[e % 3], vl[e % 3]);
                     }
                 }
             } else {
                 float vh[3], vl[3];
 #pragma unroll
                 for (int cc = 0; cc < 3; cc++) {
-                    vh[cc] = xh[p + cc * np];
-                    vl[cc] = xl[p + cc * np];
+                    const float2 v = xs[p + cc * np];
+                    vh[cc] = v.x;
+                    vl[cc] = v.y;
                 }
 #pragma unroll
-                for (int e = 0; e < 9; e++) df_sub_prod(sh[e / 3], sl[e / 3], op.fh[e], op.fl[e], vh[e % 3], vl[e % 3]);
+                for (int e = 0; e < 9; e++)
+                    df_sub_prod<AL>(sh[e / 3], sl[e / 3], op.fh[e], op.fl[e], vh[e % 3], vl[e % 3]);
             }
 #pragma unroll
             for (int cc = 0; cc < 3; cc++) {
@@ -197,12 +203,27 @@ __global__ void __launch_bounds__(kDfThreads) residual_df_kernel(Geom g, const _
     }
 }
 
-DfConst split_stencil(const ConstOp<double> &op) {
+// The stencil split into float pairs; *exact: every low half is 0.
+DfConst split_stencil(const ConstOp<double> &op, bool *exact) {
     DfConst d;
+    *exact = true;
     for (int blk = 0; blk < 27; blk++)
-        for (int e = 0; e < 9; e++) split_double(op.a[blk][e], d.ah[blk][e], d.al[blk][e]);
-    for (int e = 0; e < 9; e++) split_double(op.fix[e], d.fh[e], d.fl[e]);
+        for (int e = 0; e < 9; e++) {
+            split_double(op.a[blk][e], d.ah[blk][e], d.al[blk][e]);
+            *exact = *exact && d.al[blk][e] == 0.0f;
+        }
+    for (int e = 0; e < 9; e++) {
+        split_double(op.fix[e], d.fh[e], d.fl[e]);
+        *exact = *exact && d.fl[e] == 0.0f;
+    }
     return d;
+}
+
+template <bool ELASTIC, bool AL>
+void launch_df(const Geom &g, const DfConst &d, int centre_diag, const double *b, const float2 *xs, float *r32,
+               float scale, double *partial, cudaStream_t st) {
+    const dim3 blocks((g.M2 + 31) / 32, g.N2, g.O2), blk(32, 8);
+    residual_df_kernel<ELASTIC, AL><<<blocks, blk, 0, st>>>(g, d, centre_diag, b, xs, r32, scale, partial);
 }
 
 }  // namespace
@@ -224,17 +245,22 @@ double df_norm_scale(double bsq, size_t n) {
     return std::ldexp(1.0, -(e < -120 ? -120 : (e > 120 ? 120 : e)));   // a normal float
 }
 
-void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, const double *x, float *xh,
-                        float *xl, float *r32, double scale, double *partial, double *out, cudaStream_t st) {
+void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, const double *x, float2 *xs,
+                        float *r32, double scale, double *partial, double *out, cudaStream_t st) {
     const size_t n = 3 * (size_t)g.npad;
     const unsigned sb = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32);
-    split_kernel<<<sb, 256, 0, st>>>(x, xh, xl, n);
-    const DfConst d = split_stencil(op.cop);
-    const dim3 blocks((g.M2 + 31) / 32, g.N2, g.O2), blk(32, 8);
-    if (op.cop.elastic)
-        residual_df_kernel<true><<<blocks, blk, 0, st>>>(g, d, op.cop.centre_diag, b, xh, xl, r32, (float)scale, partial);
-    else
-        residual_df_kernel<false><<<blocks, blk, 0, st>>>(g, d, op.cop.centre_diag, b, xh, xl, r32, (float)scale, partial);
+    split_kernel<<<sb, 256, 0, st>>>(x, xs, n);
+    bool exact = false;
+    const DfConst d = split_stencil(op.cop, &exact);
+    const int cd = op.cop.centre_diag;
+    const float sc = (float)scale;
+    if (op.cop.elastic) {
+        if (exact) launch_df<true, false>(g, d, cd, b, xs, r32, sc, partial, st);
+        else launch_df<true, true>(g, d, cd, b, xs, r32, sc, partial, st);
+    } else {
+        if (exact) launch_df<false, false>(g, d, cd, b, xs, r32, sc, partial, st);
+        else launch_df<false, true>(g, d, cd, b, xs, r32, sc, partial, st);
+    }
     if (out) launch_sum_partials(partial, residual_blocks(g), out, st);
 }
 

@@ -176,21 +176,26 @@ def test_solution_matches_reference_solver(precision, kind, oracle_port):
     assert err <= SOLUTION_RTOL, f"{precision}/{kind}: {cycles} cycles, error {err:.3e}"
 
 
-@pytest.mark.parametrize("kind", ["const", "trans"])
+@pytest.mark.parametrize("kind", ["const", "const_inexact", "trans"])
 def test_double_float_residual_matches_fp64(kind, monkeypatch):
     """The mixed solver's top-level residual in double-float arithmetic (FP32
     pairs, exact products, compensated sums): after 3, 6, 9 and 12 cycles the
     relative residual it reports equals the FP64 residual norm of the same x
     to 1e-3 of itself plus 1e-13, and a solve with the FP64 residual kernel
     (STZ_MG_DF=0) takes the same number of cycles to a solution within 1e-10
-    of it (both stop at a relative residual near 1e-10).  64x64x65, dx = 1/64, the elastic and a full non-symmetric shared
-    stencil."""
+    of it (both stop at a relative residual near 1e-10).  64x64x65,
+    dx = 1/64: a full non-symmetric shared stencil, and the elastic one with
+    mu = 1, lambda = 2 (every coefficient exact in FP32: the kernel without
+    low coefficient halves) and with mu = 1.1, lambda = 2.3 (with them)."""
     import stzpp_gb300 as sg
     dims, per = (64, 64, 65), (True, True, False)
     m, n, o = dims
     dx, dy, dz = P.grid_spacing(m, n, o, per)
     b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, dx, dy, dz)
-    st, fix = sg.elastic_stencil(1.0, 2.0, dx, dy, dz) if kind == "const" else trans_stencil(2, dx)
+    if kind == "trans":
+        st, fix = trans_stencil(2, dx)
+    else:
+        st, fix = sg.elastic_stencil(*((1.0, 2.0) if kind == "const" else (1.1, 2.3)), dx, dy, dz)
     for cap in (3, 6, 9, 12):
         with sg.Multigrid(dims, per, precision="mixed") as mg:
             mg.setup_matrices(stencil=st, fix=fix)
