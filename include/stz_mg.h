@@ -48,7 +48,10 @@ typedef struct stz_mg_handle_s *stz_mg_handle;
 typedef struct {
     int m, n, o;
     int x_prd, y_prd, z_prd;
-    int precision;      /* STZ_MG_FP64 or STZ_MG_MIXED (FP32 cycles inside FP64 defect correction) */
+    int precision;      /* STZ_MG_FP64 or STZ_MG_MIXED (FP32 cycles inside FP64 defect correction; the
+                         * correction's residual of a shared-stencil top level is formed in double-float
+                         * arithmetic from the FP64 x and b, to about 1e-13 of sum |a x| per row;
+                         * STZ_MG_DF=0 in the environment forms it in FP64) */
     int v_down, v_up;   /* sweeps per level: v_down+i down, v_up+i-1 up (multigrid.hh:123, multigrid.cc:265,288) */
     int max_coarse;     /* coarsen while the coarsest level has more nodes (reference: 1024, multigrid.cc:40) */
     int bottom;         /* STZ_MG_BOTTOM_DIRECT (FP64 dense solve) or STZ_MG_BOTTOM_GS */
@@ -120,7 +123,8 @@ int stz_mg_stress_update(stz_mg_handle h, double *sigma, double lam, double mu, 
                          double dz, double *proj_mag, int where);
 
 /* multigrid::v_cycle (multigrid.cc:253-297).  In mixed precision one call is
- * one defect-correction step: FP64 residual, one FP32 V-cycle, FP64 update. */
+ * one defect-correction step: top-level residual, one FP32 V-cycle, FP64
+ * update. */
 int stz_mg_vcycle(stz_mg_handle h);
 
 /* V-cycles until |b - A x|_2 <= rel_tol |b|_2 (the loop of
@@ -129,7 +133,7 @@ int stz_mg_vcycle(stz_mg_handle h);
  * STZ_MG_ERR_NOCONV when max_cycles is reached first. */
 int stz_mg_solve(stz_mg_handle h, double rel_tol, int max_cycles, int *cycles, double *relres);
 
-/* Counters of the last stz_mg_solve: V-cycles, top-level FP64 residual
+/* Counters of the last stz_mg_solve: V-cycles, top-level residual
  * evaluations, and kernels this library launched (no counterpart in the
  * reference; its drivers time v_cycle only, shear_sim_3d.cpp:568-571). */
 int stz_mg_solve_stats(stz_mg_handle h, int *vcycles, int *residuals, long long *kernel_launches);

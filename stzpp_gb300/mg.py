@@ -327,7 +327,7 @@ class Multigrid:
         return c.value, r.value
 
     def solve_stats(self):
-        """(V-cycles, FP64 residual evaluations, kernels launched) of the last solve."""
+        """(V-cycles, top-level residual evaluations, kernels launched) of the last solve."""
         c, r, k = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
         _check(load_library().stz_mg_solve_stats(self._h, ctypes.byref(c), ctypes.byref(r), ctypes.byref(k)))
         return c.value, r.value, k.value
