@@ -25,6 +25,7 @@ sharded in this build.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -76,26 +77,37 @@ def traffic_from_profile(name):
 
 
 class Clocks:
-    """nvidia-smi clock / throttle sampling during a timed region."""
+    """nvidia-smi clock / throttle sampling around a timed region: the sampler
+    starts before the warm-up (nvidia-smi takes a moment to come up), samples
+    every 50 ms, and only the samples stamped between mark() and stop() count
+    (all samples if the stamps cannot be read)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=50):
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
         self.proc = None
+        self.t0 = None
 
     def start(self):
         self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+                 "-lms", str(self.interval_ms)], stdout=self.out, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
+    def mark(self):
+        """The timed region starts now."""
+        self.t0 = datetime.datetime.now()
+
     def stop(self):
+        t1 = datetime.datetime.now()
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -104,26 +116,42 @@ class Clocks:
         except Exception:
             self.proc.kill()
         self.out.flush()
-        rows = [l.strip().split(",") for l in open(self.out.name) if l.strip()]
+        lines = [l for l in open(self.out.name) if l.strip()]
         os.unlink(self.out.name)
-        sm, mx, reasons = [], 0.0, set()
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for r in rows:
-            r = [v.strip() for v in r]
-            if len(r) < 9:
+        return self.summarise(lines, self.t0, t1)
+
+    @classmethod
+    def summarise(cls, lines, t0, t1):
+        """Median SM clock, max clock and active throttle reasons of the
+        sample lines stamped within [t0, t1] (of every line when no stamp in
+        the window can be read)."""
+        rows = []
+        for l in lines:
+            r = [v.strip() for v in l.split(",")]
+            if len(r) < 10:
                 continue
             try:
-                sm.append(float(r[1]))
-                mx = max(mx, float(r[2]))
+                sm, mx = float(r[2]), float(r[3])
             except ValueError:
                 continue
-            for n, v in zip(names, r[5:9]):
+            try:
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                ts = None
+            rows.append((ts, sm, mx, r[6:10]))
+        window = "timed region"
+        inside = [x for x in rows if t0 is not None and x[0] is not None and t0 <= x[0] <= t1]
+        if not inside:
+            inside, window = rows, "sampler lifetime (warm-up and timed region)"
+        if not inside:
+            return None
+        reasons = set()
+        for _, _, _, flags in inside:
+            for n, v in zip(cls.REASONS, flags):
                 if v.lower().startswith("active"):
                     reasons.add(n)
-        if not sm:
-            return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(x[1] for x in inside), "sm_max_mhz": max(x[2] for x in inside),
+                "reasons": sorted(reasons), "samples": len(inside), "window": window}
 
 
 def reduce_max(value, dist, device):
@@ -247,11 +275,12 @@ def run_ours(args, world, rank, local):
         M.set_x(zero)
         return M.solve(TOL, 200)
 
+    clocks = Clocks(local)
+    clocks.start()
     for _ in range(args.warmup):
         step(mg)
-    clocks = Clocks(local)
     barrier()
-    clocks.start()
+    clocks.mark()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     cycles = 0
@@ -617,11 +646,12 @@ def run_advection(args, local, n=256, dt=200.0):
     stream = torch.cuda.current_stream()
     yielded = advect.advection_step(f, dims, sp, prm, dt, work=work)
     plastic = float((f["ad_dpl"].reshape((n + 4,) * 3)[2:-2, 2:-2, 2:-2] > 0).double().mean())
+    clocks = Clocks(local)
+    clocks.start()
     for _ in range(args.warmup):
         advect.advection_step(f, dims, sp, prm, dt, work=work, wait=False)
-    clocks = Clocks(local)
     torch.cuda.synchronize()
-    clocks.start()
+    clocks.mark()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
