@@ -331,6 +331,9 @@ def run_ours(args, world, rank, local):
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "peak_kind": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if hbm_kind == "measured" else hbm_kind,
                 "traffic": traffic_from_profile("gs_const_kernel<float>"),
+                "traffic_note": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of colour 0 repeated alone "
+                                 "(profiles/gs_const_fine_256x256x257.md): an upper bound for the in-sweep "
+                                 "average, where each pass starts on data the previous one left in L2"),
                 "algorithmic_bytes_per_launch": gs_bytes, "ms_per_launch": gs_ms,
                 "launches_per_solve": gs_launches,
                 "share_of_solve_est": gs_launches * gs_ms / ms_mixed}
