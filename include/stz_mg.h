@@ -52,8 +52,8 @@ typedef struct {
                          * correction's residual of a shared-stencil top level is formed in double-float
                          * arithmetic from the FP64 x and b, to about 1e-13 of sum |a x| per row;
                          * STZ_MG_DF=0 in the environment forms it in FP64.  Mixed precision needs
-                         * b, x and A x inside FP32's range; beyond it the solve stops with
-                         * STZ_MG_ERR_NONFINITE) */
+                         * b, x and A x inside FP32's normal range: above it the solve stops with
+                         * STZ_MG_ERR_NONFINITE, below it values count as zero) */
     int v_down, v_up;   /* sweeps per level: v_down+i down, v_up+i-1 up (multigrid.hh:123, multigrid.cc:265,288) */
     int max_coarse;     /* coarsen while the coarsest level has more nodes (reference: 1024, multigrid.cc:40) */
     int bottom;         /* STZ_MG_BOTTOM_DIRECT (FP64 dense solve) or STZ_MG_BOTTOM_GS */
