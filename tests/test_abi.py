@@ -70,3 +70,50 @@ def test_create_without_gpu_fails_cleanly(lib):
     h = ctypes.c_void_p()
     assert lib.stz_mg_create(ctypes.byref(d), ctypes.byref(h)) == 2   # STZ_MG_ERR_CUDA
     assert not h.value
+
+
+def prototypes():
+    """{name: [parameter kind, ...]} of the header's function declarations,
+    kinds 'ptr', 'int', 'double', 'longlong'."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for m in re.finditer(r"\b(stz_mg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text, flags=re.S):
+        name, params = m.group(1), " ".join(m.group(2).split())
+        kinds = []
+        if params not in ("", "void"):
+            for p in params.split(","):
+                p = p.strip()
+                if "*" in p or p.split()[0] in ("stz_mg_handle",):
+                    kinds.append("ptr")
+                elif re.search(r"\blong long\b", p):
+                    kinds.append("longlong")
+                elif re.search(r"\bdouble\b", p):
+                    kinds.append("double")
+                elif re.search(r"\bint\b", p):
+                    kinds.append("int")
+                else:
+                    kinds.append("other:" + p)
+        out[name] = kinds
+    return out
+
+
+def _kind(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return "ptr"
+    return {ctypes.c_int: "int", ctypes.c_double: "double", ctypes.c_longlong: "longlong"}.get(t, "other")
+
+
+def test_python_argtypes_match_the_header(lib):
+    """Every ctypes signature the Python binding declares has the header's
+    parameter count and kinds (a drifted signature would pass wrong values)."""
+    protos = prototypes()
+    checked = 0
+    for name, kinds in protos.items():
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is None:
+            continue
+        assert [_kind(t) for t in argtypes] == kinds, name
+        checked += 1
+    assert checked >= len(protos) - 2   # all but stz_mg_desc_default and stz_mg_last_error
