@@ -16,6 +16,12 @@
  * last error on the calling thread is stz_mg_last_error().  The reference
  * aborts the MPI job instead (p_fatal_error, common.cc:52).  A handle is not
  * thread safe; all work of a handle runs on its CUDA stream.
+ *
+ * Device pointers (where = STZ_MG_DEVICE): the caller's writes to an input
+ * must be complete before the call (synchronise the stream that produced
+ * it), and every call that reads or writes caller memory synchronises the
+ * handle's stream before it returns, so inputs may be freed or reused and
+ * outputs read on any stream as soon as the call returns.
  */
 #ifndef STZ_MG_H
 #define STZ_MG_H

@@ -59,18 +59,57 @@ inline void block9(const M &a, double *o) {
 }
 
 // Host mirror of the top region's solution, laid out like region::x0 with
-// mg = m, ng = n (no ghost layers), refreshed by multigrid_gpu::sync_x().
+// mg = m, ng = n (no ghost layers).  The mirror is filled lazily: a V-cycle
+// only marks it stale, and the first read of x0 afterwards copies the
+// solution from the device once.  So the drivers' loop of v_cycle() and
+// l2_error_all() (shear_sim_3d.cpp:567-599) moves one scalar per call, not
+// the whole field, and the solution crosses to the host once, when the
+// driver reads it (shear_sim_3d.cpp:616-674).
 template <class V>
 struct top_region {
-    V *x0 = nullptr;
+    // x0 behaves like region::x0 (a V*): x0 + offset, x0[offset], *x0, and
+    // conversion to V*; each access refreshes a stale mirror first.
+    struct lazy_x0 {
+        top_region *r = nullptr;
+        V *get() const { return r->fresh(); }
+        operator V *() const { return get(); }
+        V *operator+(std::ptrdiff_t o) const { return get() + o; }
+        V &operator[](std::ptrdiff_t o) const { return get()[o]; }
+        V &operator*() const { return *get(); }
+    };
+    lazy_x0 x0;
     int mg = 0, ng = 0, mng = 0;
     stz_mg_handle h = nullptr;
-    // region::l2_error_all as shipped (sum of |r|^4, region.cc:3030-3057)
+    // region::l2_error_all as shipped (sum of |r|^4, region.cc:3030-3057),
+    // reduced on the device
     double l2_error_all() const {
         double v = 0;
         check(stz_mg_l2_error_all(h, &v));
         return v;
     }
+    // marks the mirror stale (the device solution changed)
+    void invalidate() { stale_ = true; }
+    V *fresh() {
+        if (stale_) {
+            std::vector<double> x(3 * host_.size());
+            check(stz_mg_get_x(h, x.data(), STZ_MG_HOST));
+            for (size_t p = 0; p < host_.size(); p++) {
+                host_[p].x = x[3 * p];
+                host_[p].y = x[3 * p + 1];
+                host_[p].z = x[3 * p + 2];
+            }
+            stale_ = false;
+        }
+        return host_.data();
+    }
+    void resize(size_t n) {
+        host_.assign(n, V());
+        stale_ = true;
+    }
+
+   private:
+    std::vector<V> host_;
+    bool stale_ = true;
 };
 
 template <class V, class M>
@@ -98,8 +137,8 @@ class multigrid_gpu {
         top_.mg = m_;
         top_.ng = n_;
         top_.mng = m_ * n_;
-        xhost_.assign(npts(), V());
-        top_.x0 = xhost_.data();
+        top_.resize(npts());
+        top_.x0.r = &top_;
         reg[0] = &top_;
     }
     ~multigrid_gpu() { stz_mg_destroy(h_); }
@@ -168,12 +207,13 @@ class multigrid_gpu {
                 }
         check(stz_mg_set_x(h_, x.data(), STZ_MG_HOST));
         check(stz_mg_set_rhs(h_, r.data(), STZ_MG_HOST));
+        top_.invalidate();
     }
 
-    // multigrid::v_cycle; the host mirror reg[0]->x0 is refreshed.
+    // multigrid::v_cycle; the host mirror reg[0]->x0 refreshes on its next read.
     void v_cycle() {
         check(stz_mg_vcycle(h_));
-        sync_x();
+        top_.invalidate();
     }
 
     // V-cycles to |b - A x| <= tol |b| (the projection_step loop with the true residual).
@@ -182,19 +222,13 @@ class multigrid_gpu {
         double rr = 0;
         check(stz_mg_solve(h_, tol, max_cycles, &c, &rr));
         if (relres) *relres = rr;
-        sync_x();
+        top_.invalidate();
         return c;
     }
 
-    void sync_x() {
-        std::vector<double> x(3 * npts());
-        check(stz_mg_get_x(h_, x.data(), STZ_MG_HOST));
-        for (size_t p = 0; p < npts(); p++) {
-            xhost_[p].x = x[3 * p];
-            xhost_[p].y = x[3 * p + 1];
-            xhost_[p].z = x[3 * p + 2];
-        }
-    }
+    // Copies the solution to the host mirror now (it otherwise happens on the
+    // first read of reg[0]->x0).
+    void sync_x() { top_.fresh(); }
 
     stz_mg_handle handle() const { return h_; }
 
@@ -220,7 +254,6 @@ class multigrid_gpu {
     bool px_ = false, py_ = false, pz_ = false;
     stz_mg_handle h_ = nullptr;
     top_region<V> top_;
-    std::vector<V> xhost_;
 };
 
 }  // namespace stz_mg

@@ -10,7 +10,7 @@ oracle/_ref/trans_stencil_gen.cc, and compiled with the reference's
 stenc_funcs.hh into oracle/_ref/libtransstencil.so.  Needs the reference
 checkout; run
 
-    python oracle/trans_stencil.py /root/reference/src
+    python oracle/trans_stencil.py <reference checkout>/src
 
 The library exports
     void ref_trans_stencil(const double *T, double mu, double lamb,
@@ -68,7 +68,10 @@ def generate(cases):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    if len(sys.argv) > 1:
+        src = sys.argv[1]
+    else:
+        src = os.path.join(os.environ.get("STZPP_REFERENCE", "/root/reference"), "src")
     if not os.path.exists(os.path.join(src, "stenc_funcs.hh")):
         sys.exit(f"reference sources not found at {src}")
     cases = parse_switch(src)

@@ -79,9 +79,9 @@ class ProjectionSolver:
             _, tm, _, tl = self._key
             if self._tag(mu) == tm and self._tag(lam) == tl:
                 return
+        mu_in, lam_in = mu.detach().contiguous(), lam.detach().contiguous()
         torch.cuda.current_stream(self.device).synchronize()
-        self.mg.setup_matrices(mu=mu.detach().contiguous(), lam=lam.detach().contiguous(), spacing=self.spacing,
-                               dt=self.dt)
+        self.mg.setup_matrices(mu=mu_in, lam=lam_in, spacing=self.spacing, dt=self.dt)
         self._key = (mu, self._tag(mu), lam, self._tag(lam))
         self.stats["setups"] += 1
 
@@ -93,8 +93,9 @@ class ProjectionSolver:
         float64 CUDA tensor), assembled on the device by the solver's kernel
         (the r_field of shear_sim_3d); returns a new (npts, 3) tensor.  Uses
         the handle's right-hand side as scratch."""
+        eps_in = eps.detach().contiguous()
         torch.cuda.current_stream(self.device).synchronize()
-        self.mg.set_rhs_divergence(eps.detach().contiguous(), self.spacing)
+        self.mg.set_rhs_divergence(eps_in, self.spacing)
         out = torch.empty((self.npts, 3), dtype=torch.float64, device=self.device)
         self.mg.get_rhs(out)
         return out
@@ -118,12 +119,14 @@ class ProjectionSolve(torch.autograd.Function):
         _check_field(lam, (N,), "lam")
         solver.set_coefficients(mu, lam)
         mg = solver.mg
+        # Inputs are made on torch's stream and read on the handle's: every
+        # tensor the handle reads exists before the synchronize, and each
+        # call below returns only after the handle's stream has read it.
+        b_in = b.detach().contiguous()
+        x_in = torch.zeros_like(b) if x0 is None else x0.detach().contiguous()
         torch.cuda.current_stream(solver.device).synchronize()
-        mg.set_rhs(b.detach().contiguous())
-        if x0 is None:
-            mg.set_x(torch.zeros_like(b))
-        else:
-            mg.set_x(x0.detach().contiguous())
+        mg.set_rhs(b_in)
+        mg.set_x(x_in)
         cycles, _ = mg.solve(solver.tol, solver.max_cycles)
         solver.stats["forward_cycles"] += cycles
         u = torch.empty_like(b)
@@ -137,8 +140,9 @@ class ProjectionSolve(torch.autograd.Function):
         u, mu, lam = ctx.saved_tensors
         solver = ctx.solver
         solver.set_coefficients(mu, lam)
+        g_in = gu.contiguous()
         torch.cuda.current_stream(solver.device).synchronize()
-        w, cycles, _ = solver.mg.adjoint_solve(gu.contiguous(), tol=solver.tol, max_cycles=solver.max_cycles)
+        w, cycles, _ = solver.mg.adjoint_solve(g_in, tol=solver.tol, max_cycles=solver.max_cycles)
         solver.stats["adjoint_cycles"] += cycles
         dmu = dlam = None
         if ctx.needs_input_grad[1] or ctx.needs_input_grad[2]:

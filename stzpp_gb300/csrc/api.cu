@@ -121,6 +121,12 @@ struct stz_mg_handle_s {
     int tail_lo = -1, tail_cluster = 0, tail_cap_planes = 0;
     int stat_cycles = 0, stat_residuals = 0;
     long long stat_launches = 0;
+    // C-ABI calls on this handle so far; l2_error_all records the call that
+    // computed its value, and the residual it left in the FP32 top-level
+    // right-hand side (mixed precision) stays valid only while no other
+    // call has run since
+    long long api_calls = 0, l2_call = -1;
+    double l2_value = 0.0;
     std::vector<void *> allocs;
 
     template <typename T>
@@ -154,7 +160,10 @@ namespace {
 template <typename F>
 int guarded(stz_mg_handle h, F &&f) {
     try {
-        if (h) CK(cudaSetDevice(h->d.device));
+        if (h) {
+            h->api_calls++;
+            CK(cudaSetDevice(h->d.device));
+        }
         f();
         return STZ_MG_OK;
     } catch (const ApiError &e) {
@@ -323,6 +332,29 @@ __global__ void sumsq_partial_kernel(const double *__restrict__ v, size_t n, dou
     double s = 0.0;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
         s += v[t] * v[t];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < blockDim.x / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
+// region::l2_error_all for vec3 (region.cc:3030-3057): sum over nodes of
+// mg3d_mod_sq(|r|^2) = |r|^4, from the colour-blocked FP64 residual (3 planes
+// of npad; the slots of no node hold zero).  One partial per block, fixed
+// grid and order: deterministic.
+template <typename R>
+__global__ void quartic_partial_kernel(const R *__restrict__ res, int npad, double *__restrict__ partial) {
+    __shared__ double red[8];
+    double s = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npad; t += gridDim.x * blockDim.x) {
+        const double a = res[t], b = res[t + npad], c = res[t + 2 * (size_t)npad];
+        const double q = a * a + b * b + c * c;
+        s += q * q;
+    }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -1027,7 +1059,7 @@ int stz_mg_set_rhs(stz_mg_handle h, const double *r, int where) {
         launch_nat_to_cb<double>(g, src, h->L64[0].r, h->st);
         check_launch();
         h->bnorm = -1.0;
-        if (where == STZ_MG_HOST) sync(h);
+        sync(h);   // the caller may reuse or free r once this returns
     });
 }
 
@@ -1038,7 +1070,7 @@ int stz_mg_set_x(stz_mg_handle h, const double *x, int where) {
         const double *src = to_device(h, x, 3 * npts(g), where);
         launch_nat_to_cb<double>(g, src, h->L64[0].x, h->st);
         check_launch();
-        if (where == STZ_MG_HOST) sync(h);
+        sync(h);   // the caller may reuse or free x once this returns
     });
 }
 
@@ -1050,6 +1082,7 @@ int stz_mg_get_x(stz_mg_handle h, double *x, int where) {
         if (where == STZ_MG_DEVICE) {
             launch_cb_to_nat<double>(g, h->L64[0].x, x, h->st);
             check_launch();
+            sync(h);   // x is complete when this returns, whatever stream reads it next
         } else {
             double *d = staging(h, n);
             launch_cb_to_nat<double>(g, h->L64[0].x, d, h->st);
@@ -1120,7 +1153,9 @@ int stz_mg_vcycle(stz_mg_handle h) {
         if (h->d.precision == STZ_MG_FP64) {
             run_vcycle64(h, 1);
         } else {
-            top_residual_sq(h, h->L32[0].r);
+            // a stz_mg_l2_error_all call just before left b - A x of the
+            // current x in the FP32 right-hand side
+            if (h->l2_call != h->api_calls - 1) top_residual_sq(h, h->L32[0].r);
             mixed_step(h, 1);
         }
         sync(h);
@@ -1235,22 +1270,32 @@ int stz_mg_l2_error_all(stz_mg_handle h, double *out) {
     if (!h || !out) return set_error(STZ_MG_ERR_ARG, "null argument");
     return guarded(h, [&] {
         need_setup(h);
-        const Geom &g = h->geo[0];
-        const size_t n = 3 * npts(g);
-        launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L64[0].res, nullptr, nullptr,
-                                        h->st);
-        check_launch();
-        double *nat = staging(h, n);
-        launch_cb_to_nat<double>(g, h->L64[0].res, nat, h->st);
-        std::vector<double> v(n);
-        CK(cudaMemcpyAsync(v.data(), nat, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-        sync(h);
-        double s = 0;
-        for (size_t p = 0; p < n; p += 3) {
-            double q = v[p] * v[p] + v[p + 1] * v[p + 1] + v[p + 2] * v[p + 2];
-            s += q * q;
+        if (h->l2_call == h->api_calls - 1) {   // nothing has run since the last evaluation
+            h->l2_call = h->api_calls;
+            *out = h->l2_value;
+            return;
         }
-        *out = s;
+        const Geom &g = h->geo[0];
+        const int nb = std::min(h->partial_len, 4 * 152);
+        if (h->d.precision == STZ_MG_FP64) {
+            // FP64 residual into the top level's res field, then a device sum of |r|^4
+            launch_residual<double, double>(h->op64[0], g, h->L64[0].r, h->L64[0].x, h->L64[0].res, nullptr,
+                                            nullptr, h->st);
+            quartic_partial_kernel<double><<<nb, 256, 0, h->st>>>(h->L64[0].res, g.npad, h->partial);
+        } else {
+            // the residual the next defect-correction step starts from (FP32
+            // top-level right-hand side, formed exactly as stz_mg_vcycle forms
+            // it), summed as |r|^4 in FP64; stz_mg_vcycle then reuses it
+            top_residual_sq(h, h->L32[0].r);
+            quartic_partial_kernel<float><<<nb, 256, 0, h->st>>>(h->L32[0].r, g.npad, h->partial);
+        }
+        sum_blocks_kernel<<<1, 1024, 0, h->st>>>(h->partial, nb, h->dscal);
+        check_launch();
+        CK(cudaMemcpyAsync(h->hscal, h->dscal, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+        if (!std::isfinite(h->hscal[0])) fail(STZ_MG_ERR_NONFINITE, "residual is not finite");
+        *out = h->l2_value = h->hscal[0];
+        h->l2_call = h->api_calls;
     });
 }
 

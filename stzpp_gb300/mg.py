@@ -130,6 +130,10 @@ def _arg(a, n=None):
         if n is not None and a.numel() != n:
             raise ValueError(f"expected {n} elements, got {a.numel()}")
         if a.is_cuda:
+            # the handle's stream reads or writes this memory: torch's work on
+            # it (producing an input, or still reading a recycled output
+            # block) must be finished first
+            torch.cuda.current_stream(a.device).synchronize()
             return ctypes.c_void_p(a.data_ptr()), DEVICE, a
         a = a.numpy()
     arr = np.ascontiguousarray(a, dtype=np.float64)

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <random>
 #include <vector>
 
@@ -130,11 +131,52 @@ int run(int N, const char *dump) {
     return rel <= 1e-10 ? 0 : 1;
 }
 
+// The projection_step loop of shear_sim_3d.cpp:565-599 verbatim in its
+// calls: v_cycle() and reg[0]->l2_error_all() (twice once the cycle count
+// reaches std_iters/16) until the sum of |r|^4 drops below
+// (1e3 eps stencil[13].a11)^2, then two more v_cycle()s; the solution is
+// read through reg[0]->x0 afterwards.  Prints "cycles relres checksum".
+template <class M>
+int run_driver_loop(int N) {
+    sim<M> s(N);
+    stz_mg::multigrid_gpu<vec3, M> mgrid(s);
+    mgrid.setup_matrices(s);
+    mgrid.setup_fields(s);
+    const double a11 = s.stencil[13].a11;
+    double tol = std::numeric_limits<double>::epsilon() * a11 * 1e3;
+    tol *= tol;
+    const int std_iters = 16;
+    int num_iters = 1, cycles = 0;
+    double err = 1e16;
+    while (err > tol && cycles < 100) {
+        mgrid.v_cycle();
+        cycles++;
+        err = mgrid.reg[0]->l2_error_all();
+        if (num_iters >= std_iters / 16) err = mgrid.reg[0]->l2_error_all();
+        num_iters++;
+    }
+    mgrid.v_cycle();
+    mgrid.v_cycle();
+    cycles += 2;
+    auto *top = mgrid.reg[0];
+    double cs = 0;
+    for (int k = 0; k <= N; k++)
+        for (int j = 0; j < N; j++)
+            for (int i = 0; i < N; i++) {
+                const vec3 *v = top->x0 + i + top->mg * (j + top->ng * k);
+                cs += v->x * 1.0 + v->y * 2.0 + v->z * 3.0;
+            }
+    double rn = 0, bn = 0;
+    stz_mg::check(stz_mg_residual_norm(mgrid.handle(), &rn, &bn));
+    std::printf("%d %.3e %.12e\n", cycles, rn / bn, cs);
+    return err <= tol ? 0 : 1;
+}
+
 int main(int argc, char **argv) {
     int N = argc > 1 ? std::atoi(argv[1]) : 16;
     try {
         const char *dump = argc > 2 ? argv[2] : nullptr;
-        return run<mat3>(N, dump) | run<sym_mat3>(N, nullptr);
+        return run<mat3>(N, dump) | run<sym_mat3>(N, nullptr) | run_driver_loop<mat3>(N);
     } catch (const stz_mg::error &e) {
         std::fprintf(stderr, "stz_mg error %d: %s\n", e.code, e.what());
         return 2;

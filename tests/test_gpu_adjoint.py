@@ -190,3 +190,27 @@ def test_checkpointed_sequence_matches_stored():
     assert abs(res[0][0] - res[2][0]) <= 1e-12 * abs(res[0][0])
     for a, c in zip(res[2][1:], res[0][1:]):
         assert rel(a, c) <= 1e-9
+
+
+def test_forward_output_is_ready_on_torch_stream_256():
+    """The solver works on its own stream; the tensor forward returns must be
+    complete when torch's stream reads it straight away (256x256x257, so a
+    missing synchronisation would show)."""
+    import torch
+    from stzpp_gb300.autograd import ProjectionSolver
+    dims, per = (256, 256, 257), (True, True, False)
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per)
+    cuda = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    b = cuda(P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h))
+    mu = torch.ones(m * n * o, dtype=torch.float64, device="cuda")
+    lam = 2 * mu
+    S = ProjectionSolver(dims, per, h, precision="mixed", tol=1e-8)
+    u = S(b, mu, lam)
+    early = u.clone()            # queued on torch's stream right after forward
+    s1 = float(u.abs().sum())
+    torch.cuda.synchronize()
+    late = S.mg.get_x()          # the handle's solution, read back after a full synchronize
+    S.close()
+    assert np.array_equal(early.cpu().numpy(), late)
+    assert s1 == float(np.abs(late).sum()) or abs(s1 - float(np.abs(late).sum())) <= 1e-12 * s1
