@@ -42,8 +42,18 @@ def _load():
     lib.so_residual.argtypes = [vp, ci, vp, vp]
     lib.so_solve.argtypes = [vp, ctypes.c_double, ci, ci, ci, vp, vp]
     lib.so_set_cycle.argtypes = [vp, ci, ci, ci, ci]
+    lib.so_set_threads.argtypes = [ci]
+    lib.so_threads.restype = ci
     _lib = lib
     return lib
+
+
+def set_threads(n: int) -> int:
+    """Host threads of every handle (1: the serial restatement; P > 1: the
+    reference's z-decomposed sweep on P slabs).  Returns the count in effect."""
+    lib = _load()
+    lib.so_set_threads(int(n))
+    return lib.so_threads()
 
 
 def available() -> bool:
@@ -138,6 +148,12 @@ class PortMultigrid:
         sq = ctypes.c_double()
         self._check(_load().so_residual(self._h, l, _ptr(out), ctypes.byref(sq)))
         return out, sq.value
+
+    def residual_sq(self, l=0):
+        """|r - A x|^2 of level l without copying the residual out."""
+        sq = ctypes.c_double()
+        self._check(_load().so_residual(self._h, l, None, ctypes.byref(sq)))
+        return sq.value
 
     def solve(self, tol=1e-10, max_cycles=100, bottom="gs", smoother="lex"):
         hist = np.zeros(max_cycles)

@@ -15,6 +15,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #define MAXLEV 16
 #define BOUND_LOW (-1024) /* common.hh:41-42 */
 #define BOUND_HIGH 1024
@@ -30,6 +34,23 @@ static int fail(const char *fmt, ...) {
 }
 
 const char *so_last_error(void) { return g_err; }
+
+/* Host threads of the sweeps, transfers and RAT (1: the serial restatement).
+ * With P > 1 a level of o planes is split into min(P, o/8) z-slabs, each
+ * swept lexicographically by its own thread with every value outside the slab
+ * read from the copy taken at the start of the sweep: what the reference does
+ * on P MPI ranks decomposed along z, whose ghost layers are refreshed once per
+ * sweep (region.cc:1600, communicate region.cc:2759-2847). */
+static int g_threads = 1;
+
+void so_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int so_threads(void) {
+#ifdef _OPENMP
+    return g_threads;
+#else
+    return 1;
+#endif
+}
 
 typedef struct {
     int m, n, o, xp, yp, zp;
@@ -111,6 +132,25 @@ static void build_fine(lev_t *L, const double *stencil, const double *fix, const
     L->aoff = xcalloc((size_t)L->npts + 1, sizeof(long));
     long nb = 0;
     int p = 0;
+    if (!pts) {
+        /* one shared stencil: every interior point refers to the same 27
+         * blocks and every Dirichlet point to the same fix block, as the
+         * simulation's external_ptr does (src/shear_sim_3d.hh:388-402) */
+        for (k = 0; k < L->o; k++)
+            for (j = 0; j < L->n; j++)
+                for (i = 0; i < L->m; i++, p++) {
+                    int in = is_interior(L, i, j, k), *S = L->S + 6 * p;
+                    S[0] = S[2] = S[4] = in ? -1 : 0;
+                    S[1] = S[3] = S[5] = in ? 2 : 1;
+                    L->aoff[p] = in ? 0 : 27;
+                }
+        L->aoff[L->npts] = 28;
+        L->A = xcalloc((size_t)9 * 28, sizeof(double));
+        memcpy(L->A, stencil, 243 * sizeof(double));
+        memcpy(L->A + 243, fix, 9 * sizeof(double));
+        alloc_fields(L);
+        return;
+    }
     for (k = 0; k < L->o; k++)
         for (j = 0; j < L->n; j++)
             for (i = 0; i < L->m; i++, p++) {
@@ -220,18 +260,14 @@ static int fine_and_coarse_box(const lev_t *P, int fi, int fj, int fk, int *fb, 
     return 0;
 }
 
+static int level_slabs(const lev_t *L);
+static int scatter_threads(const lev_t *C);
+
 /* Coarse level bounds: region ctor region.cc:853-959 and fill_rat_bounds
  * region.cc:1848-1905 (strip communication replaced by wrapping the target
  * index; box union is order independent). */
-static int build_coarse_bounds(lev_t *C, const lev_t *P) {
-    int ck, cj, ci, sx, sy, sz;
-    C->npts = C->m * C->n * C->o;
-    C->S = xcalloc((size_t)6 * C->npts, sizeof(int));
-    for (int p = 0; p < C->npts; p++) {
-        int *S = C->S + 6 * p;
-        S[0] = 0; S[1] = 1; S[2] = 0; S[3] = 1; S[4] = 0; S[5] = 1;
-    }
-    for (ck = 0; ck < C->o; ck++)
+static int bounds_plane(lev_t *C, const lev_t *P, int ck) {
+    int cj, ci, sx, sy, sz;
         for (cj = 0; cj < C->n; cj++)
             for (ci = 0; ci < C->m; ci++)
                 for (sz = 0; sz < 2; sz++)
@@ -257,6 +293,28 @@ static int build_coarse_bounds(lev_t *C, const lev_t *P) {
                                                    cb[4] - tk, cb[5] - tk);
                                     }
                         }
+    return 0;
+}
+
+static int build_coarse_bounds(lev_t *C, const lev_t *P) {
+    C->npts = C->m * C->n * C->o;
+    C->S = xcalloc((size_t)6 * C->npts, sizeof(int));
+    for (int p = 0; p < C->npts; p++) {
+        int *S = C->S + 6 * p;
+        S[0] = 0; S[1] = 1; S[2] = 0; S[3] = 1; S[4] = 0; S[5] = 1;
+    }
+    /* a box union does not depend on the order of its updates */
+    const int T = scatter_threads(C);
+    int bad = 0;
+    for (int par = 0; par < (T == 1 ? 1 : 2); par++) {
+#pragma omp parallel for num_threads(T) schedule(static) if (T > 1)
+        for (int ck = (T == 1 ? 0 : par); ck < C->o; ck += (T == 1 ? 1 : 2))
+            if (bounds_plane(C, P, ck)) {
+#pragma omp atomic write
+                bad = 1;
+            }
+    }
+    if (bad) return -1;
     C->aoff = xcalloc((size_t)C->npts + 1, sizeof(long));
     long nb = 0;
     for (int p = 0; p < C->npts; p++) {
@@ -275,9 +333,8 @@ static int build_coarse_bounds(lev_t *C, const lev_t *P) {
  * order as rt_scan_grid; contributions to wrapped targets are added directly
  * (the reference routes them through strip buffers, which only changes the
  * order of the floating-point additions). */
-static int build_coarse_coeffs(st_t *s, lev_t *C, const lev_t *P) {
-    int ck, cj, ci, sx, sy, sz, err = 0;
-    for (ck = 0; ck < C->o; ck++)
+static int rat_plane(lev_t *C, const lev_t *P, int ck, double **work, long *work_len) {
+    int cj, ci, sx, sy, sz, err = 0;
         for (cj = 0; cj < C->n; cj++)
             for (ci = 0; ci < C->m; ci++)
                 for (sz = 0; sz < 2; sz++)
@@ -288,12 +345,12 @@ static int build_coarse_coeffs(st_t *s, lev_t *C, const lev_t *P) {
                             int fb[6], cb[6];
                             if (fine_and_coarse_box(P, fi, fj, fk, fb, cb)) return -1;
                             int nJ = (cb[1] - cb[0]) * (cb[3] - cb[2]) * (cb[5] - cb[4]);
-                            if (s->work_len < 9L * nJ) {
-                                free(s->work);
-                                s->work_len = 9L * nJ;
-                                s->work = xcalloc((size_t)s->work_len, sizeof(double));
+                            if (*work_len < 9L * nJ) {
+                                free(*work);
+                                *work_len = 9L * nJ;
+                                *work = xcalloc((size_t)*work_len, sizeof(double));
                             }
-                            double *At = s->work;
+                            double *At = *work;
                             const double *Apar = P->A + 9 * P->aoff[fi + P->m * (fj + P->n * fk)];
                             int t0 = fb[1] - fb[0], t1 = fb[3] - fb[2];
                             /* A_red */
@@ -353,6 +410,31 @@ static int build_coarse_coeffs(st_t *s, lev_t *C, const lev_t *P) {
     return 0;
 }
 
+static int build_coarse_coeffs(st_t *s, lev_t *C, const lev_t *P) {
+    const int T = scatter_threads(C);
+    if (T == 1) {
+        for (int ck = 0; ck < C->o; ck++)
+            if (rat_plane(C, P, ck, &s->work, &s->work_len)) return -1;
+        return 0;
+    }
+    int bad = 0;
+    for (int par = 0; par < 2; par++) {
+#pragma omp parallel num_threads(T)
+        {
+            double *work = NULL;
+            long work_len = 0;
+#pragma omp for schedule(static)
+            for (int ck = par; ck < C->o; ck += 2)
+                if (rat_plane(C, P, ck, &work, &work_len)) {
+#pragma omp atomic write
+                    bad = 1;
+                }
+            free(work);
+        }
+    }
+    return bad ? -1 : 0;
+}
+
 /* Value of x at an unwrapped neighbour index: a periodic index outside the
  * grid reads the wrapped value from `ghost` (the lagged snapshot in a
  * Gauss-Seidel sweep, the current array elsewhere). */
@@ -367,19 +449,24 @@ static inline const double *nbr(const lev_t *L, const double *cur, const double 
 }
 
 /* One point update of region::gauss_seidel (region.cc:1557-1762):
- * x_c = inv(A_c) (r - sum_{q != c} A_q x_q), box order, centre skipped. */
-static void gs_point(lev_t *L, int i, int j, int k, const double *ghost) {
+ * x_c = inv(A_c) (r - sum_{q != c} A_q x_q), box order, centre skipped.
+ * Planes outside [k0, k1) (another sub-domain's, or a periodic image) are
+ * read from `ghost`; the whole grid is one sub-domain on one thread. */
+static void gs_point(lev_t *L, int i, int j, int k, int k0, int k1, const double *ghost) {
     int p = i + L->m * (j + L->n * k);
     const int *S = L->S + 6 * p;
     const double *Ap = L->A + 9 * L->aoff[p], *Ac = NULL;
     double Ax[3] = {0, 0, 0}, t[3];
-    for (int dk = S[4]; dk < S[5]; dk++)
+    for (int dk = S[4]; dk < S[5]; dk++) {
+        const int kk = k + dk;
+        const double *src = (kk >= k0 && kk < k1) ? L->x : ghost;
         for (int dj = S[2]; dj < S[3]; dj++)
             for (int di = S[0]; di < S[1]; di++, Ap += 9) {
                 if (di == 0 && dj == 0 && dk == 0) { Ac = Ap; continue; }
-                matvec(Ap, nbr(L, L->x, ghost, i + di, j + dj, k + dk), t);
+                matvec(Ap, nbr(L, src, ghost, i + di, j + dj, kk), t);
                 Ax[0] += t[0]; Ax[1] += t[1]; Ax[2] += t[2];
             }
+    }
     double inv[9], d[3], *x = L->x + 3 * (size_t)p;
     const double *r = L->r + 3 * (size_t)p;
     inverse3(Ac, inv);
@@ -387,13 +474,37 @@ static void gs_point(lev_t *L, int i, int j, int k, const double *ghost) {
     matvec(inv, d, x);
 }
 
+/* z-slabs of a level: min(threads, o/8), at least 1 (small levels stay on
+ * fewer threads, as the reference gathers coarse levels onto fewer ranks,
+ * multigrid.cc:47-103). */
+static int level_slabs(const lev_t *L) {
+    int P = so_threads(), cap = L->o / 8;
+    if (P > cap) P = cap;
+    return P < 1 ? 1 : P;
+}
+
 /* Lexicographic sweep with ghosts lagged to the start of the sweep
- * (communicate() once at region.cc:1600). */
+ * (communicate() once at region.cc:1600); with several slabs each is swept
+ * by one thread and reads the others' planes from the same snapshot. */
 static void gs_lex(lev_t *L) {
-    memcpy(L->xs, L->x, sizeof(double) * 3 * (size_t)L->npts);
-    for (int k = 0; k < L->o; k++)
-        for (int j = 0; j < L->n; j++)
-            for (int i = 0; i < L->m; i++) gs_point(L, i, j, k, L->xs);
+    const int P = level_slabs(L);
+    const size_t plane = (size_t)3 * L->m * L->n;
+    if (P == 1) {
+        memcpy(L->xs, L->x, sizeof(double) * 3 * (size_t)L->npts);
+        for (int k = 0; k < L->o; k++)
+            for (int j = 0; j < L->n; j++)
+                for (int i = 0; i < L->m; i++) gs_point(L, i, j, k, 0, L->o, L->xs);
+        return;
+    }
+#pragma omp parallel for num_threads(P) schedule(static)
+    for (int k = 0; k < L->o; k++) memcpy(L->xs + plane * k, L->x + plane * k, sizeof(double) * plane);
+#pragma omp parallel for num_threads(P) schedule(static, 1)
+    for (int sl = 0; sl < P; sl++) {
+        const int k0 = (int)((long)sl * L->o / P), k1 = (int)((long)(sl + 1) * L->o / P);
+        for (int k = k0; k < k1; k++)
+            for (int j = 0; j < L->n; j++)
+                for (int i = 0; i < L->m; i++) gs_point(L, i, j, k, k0, k1, L->xs);
+    }
 }
 
 /* 8-colour sweep: colour q = (i&1) + 2(j&1) + 4(k&1), q = 0..7; within a
@@ -402,7 +513,7 @@ static void gs_mc8(lev_t *L) {
     for (int q = 0; q < 8; q++)
         for (int k = (q >> 2) & 1; k < L->o; k += 2)
             for (int j = (q >> 1) & 1; j < L->n; j += 2)
-                for (int i = q & 1; i < L->m; i += 2) gs_point(L, i, j, k, L->x);
+                for (int i = q & 1; i < L->m; i += 2) gs_point(L, i, j, k, 0, L->o, L->x);
 }
 
 static void gs_sweep(lev_t *L, int smoother) {
@@ -430,45 +541,68 @@ static void residual_point(const lev_t *L, int i, int j, int k, double *out) {
  * (2129-2271): coarse r = sum over fine points of (1/8) P^T residual, the
  * weight of each fine point being 1/8 times its interpolation weight; then
  * multigrid::restriction clears the coarse x (multigrid.cc:444). */
+static void restrict_plane(lev_t *C, const lev_t *P, int ck) {
+    for (int cj = 0; cj < C->n; cj++)
+        for (int ci = 0; ci < C->m; ci++)
+            for (int sz = 0; sz < 2; sz++)
+                for (int sy = 0; sy < 2; sy++)
+                    for (int sx = 0; sx < 2; sx++) {
+                        int fi = 2 * ci + sx, fj = 2 * cj + sy, fk = 2 * ck + sz;
+                        if (fi >= P->m || fj >= P->n || fk >= P->o) continue;
+                        double res[3];
+                        residual_point(P, fi, fj, fk, res);
+                        int px[2], py[2], pz[2], cx, cy, cz;
+                        int nx = parents1d(fi, P->m, P->xp, px, &cx);
+                        int ny = parents1d(fj, P->n, P->yp, py, &cy);
+                        int nz = parents1d(fk, P->o, P->zp, pz, &cz);
+                        if (sx == 0 && sy == 1 && sz == 1) {
+                            /* restrict_partial, mask 145 (region.cc:2236-2243): the
+                             * split of this sub-point between the two y parents is
+                             * decided by the cell's x-collapse flag xs, not by ys. */
+                            int xs = !P->xp && !(P->m & 1) && ci == C->m - 2;
+                            if (xs) { py[0] = cj + 1; ny = 1; }
+                            else { py[0] = cj; py[1] = cj + 1; ny = 2; }
+                        }
+                        double w = 0.125 * (nx == 2 ? 0.5 : 1) * (ny == 2 ? 0.5 : 1) * (nz == 2 ? 0.5 : 1);
+                        double rd[3] = {w * res[0], w * res[1], w * res[2]};
+                        for (int a = 0; a < nz; a++)
+                            for (int b = 0; b < ny; b++)
+                                for (int c = 0; c < nx; c++) {
+                                    double *t = C->r + 3 * (wrap(px[c], C->m) + (size_t)C->m * (wrap(py[b], C->n) + (size_t)C->n * wrap(pz[a], C->o)));
+                                    t[0] += rd[0]; t[1] += rd[1]; t[2] += rd[2];
+                                }
+                    }
+}
+
+/* Threads for a scatter over the coarse planes ck of a level: the fine points
+ * under coarse plane ck add into coarse planes ck and ck + 1 only, so planes
+ * of one parity run in parallel and the two parities one after the other
+ * (1: serial, in the reference's order; also when a periodic z of odd extent
+ * would let the last plane's updates wrap onto plane 0). */
+static int scatter_threads(const lev_t *C) {
+    int P = level_slabs(C);
+    return (C->zp && (C->o & 1)) ? 1 : P;
+}
+
 static void restriction(lev_t *C, const lev_t *P) {
     memset(C->r, 0, sizeof(double) * 3 * (size_t)C->npts);
-    for (int ck = 0; ck < C->o; ck++)
-        for (int cj = 0; cj < C->n; cj++)
-            for (int ci = 0; ci < C->m; ci++)
-                for (int sz = 0; sz < 2; sz++)
-                    for (int sy = 0; sy < 2; sy++)
-                        for (int sx = 0; sx < 2; sx++) {
-                            int fi = 2 * ci + sx, fj = 2 * cj + sy, fk = 2 * ck + sz;
-                            if (fi >= P->m || fj >= P->n || fk >= P->o) continue;
-                            double res[3];
-                            residual_point(P, fi, fj, fk, res);
-                            int px[2], py[2], pz[2], cx, cy, cz;
-                            int nx = parents1d(fi, P->m, P->xp, px, &cx);
-                            int ny = parents1d(fj, P->n, P->yp, py, &cy);
-                            int nz = parents1d(fk, P->o, P->zp, pz, &cz);
-                            if (sx == 0 && sy == 1 && sz == 1) {
-                                /* restrict_partial, mask 145 (region.cc:2236-2243): the
-                                 * split of this sub-point between the two y parents is
-                                 * decided by the cell's x-collapse flag xs, not by ys. */
-                                int xs = !P->xp && !(P->m & 1) && ci == C->m - 2;
-                                if (xs) { py[0] = cj + 1; ny = 1; }
-                                else { py[0] = cj; py[1] = cj + 1; ny = 2; }
-                            }
-                            double w = 0.125 * (nx == 2 ? 0.5 : 1) * (ny == 2 ? 0.5 : 1) * (nz == 2 ? 0.5 : 1);
-                            double rd[3] = {w * res[0], w * res[1], w * res[2]};
-                            for (int a = 0; a < nz; a++)
-                                for (int b = 0; b < ny; b++)
-                                    for (int c = 0; c < nx; c++) {
-                                        double *t = C->r + 3 * (wrap(px[c], C->m) + (size_t)C->m * (wrap(py[b], C->n) + (size_t)C->n * wrap(pz[a], C->o)));
-                                        t[0] += rd[0]; t[1] += rd[1]; t[2] += rd[2];
-                                    }
-                        }
+    const int T = scatter_threads(C);
+    if (T == 1) {
+        for (int ck = 0; ck < C->o; ck++) restrict_plane(C, P, ck);
+    } else {
+        for (int par = 0; par < 2; par++) {
+#pragma omp parallel for num_threads(T) schedule(static)
+            for (int ck = par; ck < C->o; ck += 2) restrict_plane(C, P, ck);
+        }
+    }
     memset(C->x, 0, sizeof(double) * 3 * (size_t)C->npts);
 }
 
 /* region::interpolation (region.cc:1816-1843) with interpolate_full/partial
  * (2061-2121): fine x += P x_coarse (weights 1, 1/2, 1/4, 1/8). */
 static void interpolation(const lev_t *C, lev_t *P) {
+    const int T = level_slabs(P);
+#pragma omp parallel for num_threads(T) schedule(static) if (T > 1)
     for (int fk = 0; fk < P->o; fk++)
         for (int fj = 0; fj < P->n; fj++)
             for (int fi = 0; fi < P->m; fi++) {
@@ -576,7 +710,34 @@ static int vcycle(st_t *s, int smoother, int bottom) {
     return 0;
 }
 
+static double residual_sq_serial(const lev_t *L, double *out);
+
+/* With several threads: per-plane sums, added in plane order. */
 static double residual_sq(const lev_t *L, double *out) {
+    const int T = level_slabs(L);
+    if (T == 1) return residual_sq_serial(L, out);
+    double *part = xcalloc((size_t)L->o, sizeof(double));
+#pragma omp parallel for num_threads(T) schedule(static)
+    for (int k = 0; k < L->o; k++) {
+        double sum = 0, r[3];
+        for (int j = 0; j < L->n; j++)
+            for (int i = 0; i < L->m; i++) {
+                residual_point(L, i, j, k, r);
+                if (out) {
+                    size_t p = i + (size_t)L->m * (j + (size_t)L->n * k);
+                    out[3 * p] = r[0]; out[3 * p + 1] = r[1]; out[3 * p + 2] = r[2];
+                }
+                sum += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            }
+        part[k] = sum;
+    }
+    double sum = 0;
+    for (int k = 0; k < L->o; k++) sum += part[k];
+    free(part);
+    return sum;
+}
+
+static double residual_sq_serial(const lev_t *L, double *out) {
     double sum = 0, r[3];
     for (int k = 0; k < L->o; k++)
         for (int j = 0; j < L->n; j++)

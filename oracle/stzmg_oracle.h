@@ -43,6 +43,13 @@ int so_residual(void *h, int l, double *out, double *sq);
 int so_solve(void *h, double tol, int max_cycles, int smoother, int bottom, int *cycles,
              double *hist);
 int so_set_cycle(void *h, int v_down, int v_up, int bottom_sweeps, int grow);
+/* Host threads for every handle (default 1, the serial restatement): P > 1
+ * runs each level as min(P, o/8) z-slab sub-domains, one thread each, with
+ * the reference's per-sweep ghost refresh at the slab faces (its MPI
+ * decomposition along z); transfers, residuals and RAT run their planes in
+ * parallel.  so_threads() is the count in effect (1 without OpenMP). */
+void so_set_threads(int n);
+int so_threads(void);
 
 #ifdef __cplusplus
 }

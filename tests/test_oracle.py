@@ -272,3 +272,41 @@ def test_port_matches_live_reference_trans(frame, oracle_port):
         R.v_cycle("gs")
         Q.v_cycle(bottom="gs", smoother="lex")
     assert rel(Q.get_field(0, "x"), R.get_field(0, "x")) < 1e-11
+
+
+def test_threaded_port_matches_serial(oracle_port):
+    """The oracle on several threads (the reference's sweep on z-slab
+    sub-domains with ghosts refreshed once per sweep, as on MPI ranks split
+    along z): single transfers and residuals equal the serial ones to
+    round-off, and the converged solution is the serial one."""
+    dims, per = (32, 32, 33), (True, True, False)
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per)
+    st, fix = P.elastic_stencil_const(1.0, 2.0, *h)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    x0 = np.random.default_rng(4).standard_normal(b.shape) * 1e-4
+    out = {}
+    try:
+        for T in (1, 4):
+            assert oracle_port.set_threads(T) in (1, T)
+            Q = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix)
+            Q.set_field(0, "r", b)
+            Q.set_field(0, "x", x0)
+            res, sq = Q.residual(0)
+            Q.restriction(1)
+            r1 = Q.get_field(1, "r")
+            Q.set_field(1, "x", r1)
+            Q.interpolation(1)
+            xi = Q.get_field(0, "x")
+            Q.set_field(0, "x", np.zeros_like(b))
+            cycles, _ = Q.solve(1e-12, 100)
+            out[T] = (res, sq, r1, xi, Q.get_field(0, "x"), [Q.level_A(l) for l in range(Q.nlevels)])
+    finally:
+        oracle_port.set_threads(1)
+    s, t = out[1], out[4]
+    assert np.array_equal(s[0], t[0]) and abs(s[1] - t[1]) <= 1e-13 * s[1]
+    assert np.abs(s[2] - t[2]).max() <= 1e-14 * np.abs(s[2]).max()
+    assert np.abs(s[3] - t[3]).max() <= 1e-14 * np.abs(s[3]).max()
+    assert rel(t[4], s[4]) <= 1e-9
+    for a, c in zip(s[5], t[5]):
+        assert np.abs(a - c).max() <= 1e-13 * np.abs(a).max()
