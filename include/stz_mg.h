@@ -210,6 +210,12 @@ enum {
 };
 int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double *ms_per_launch,
                        double *work_per_launch);
+/* Measurement hook (no counterpart in the reference): how the solver sweeps
+ * a level in its precision -- STZ_MG_SWEEP_COLOUR (eight colour launches per
+ * sweep), _TILE (two-buffer tiles), _BAND (full-width bands staged by TMA),
+ * _PHASE (a block per plane) -- and the kernel launches of one sweep. */
+enum { STZ_MG_SWEEP_COLOUR = 0, STZ_MG_SWEEP_TILE = 1, STZ_MG_SWEEP_BAND = 2, STZ_MG_SWEEP_PHASE = 3 };
+int stz_mg_sweep_kind(stz_mg_handle h, int level, int *kind, int *launches_per_sweep);
 
 /* Allocation-free residual check (no counterpart in the reference).
  *
@@ -238,7 +244,9 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
  * ordering) race and corrupt each other's results, so keep them on one stream
  * or order them with events.  The first call on a device looks up the array's
  * device address (once per device); make that first call before any stream
- * capture begins. */
+ * capture begins, and do not reset the device (cudaDeviceReset) between
+ * calls: the address kept from the first call would no longer be valid.  A
+ * stream of another device than `device` is refused with STZ_MG_ERR_ARG. */
 #define STZ_MG_NOALLOC_PARTIALS 131072
 #define STZ_MG_NOALLOC_MAX_NODES (1024LL * STZ_MG_NOALLOC_PARTIALS)
 int stz_mg_const_residual_sumsq_noalloc(int m, int n, int o, int x_prd, int y_prd, int z_prd,

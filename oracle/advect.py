@@ -180,3 +180,68 @@ def reference_step(fields, nx, ny, nz, prm, dt, lx=1.0, ly=1.0, lz=1.0, zper=Fal
     finally:
         lib.adv_free(h)
     return buf
+
+
+def _ref_handle(lib, fields, nx, ny, nz, prm, zper=False, outdir="adv_harness_out"):
+    vp = ctypes.c_void_p
+    lib.adv_npoints.argtypes = [vp]
+    lib.adv_npoints.restype = ctypes.c_long
+    lib.adv_set.argtypes = lib.adv_get.argtypes = [vp, vp]
+    lib.adv_free.argtypes = [vp]
+    p = _ref_params(prm)
+    h = lib.adv_new(nx, ny, nz, 1.0, 1.0, 1.0, p.ctypes.data_as(vp), int(zper), outdir.encode())
+    assert lib.adv_npoints(h) == fields.shape[0]
+    buf = np.ascontiguousarray(fields, dtype=np.float64).copy()
+    lib.adv_set(h, buf.ctypes.data_as(vp))
+    return h, buf
+
+
+def reference_rhs(fields, nx, ny, nz, prm):
+    """The unmodified reference's r_field (shear_sim_3d.hh:283-385) of every
+    node of an nx x ny x nz cell grid (x, y periodic, z plates): (npts, 3),
+    nodes in natural order with nz + 1 node planes."""
+    lib = _ref_lib()
+    vp = ctypes.c_void_p
+    lib.adv_rhs.argtypes = [vp, vp]
+    h, _ = _ref_handle(lib, fields, nx, ny, nz, prm)
+    try:
+        out = np.zeros((nx * ny * (nz + 1), 3))
+        lib.adv_rhs(h, out.ctypes.data_as(vp))
+    finally:
+        lib.adv_free(h)
+    return out
+
+
+def reference_projection(fields, nx, ny, nz, prm, dt):
+    """The unmodified reference's quasi-static projection step
+    (shear_sim_3d::projection_step, shear_sim_3d.cpp:528-724: multigrid solve
+    for the velocities, then the stress update) on a copy of fields;
+    returns (new fields, proj_mag)."""
+    lib = _ref_lib()
+    vp = ctypes.c_void_p
+    lib.adv_project.argtypes = [vp, ctypes.c_double]
+    lib.adv_project.restype = ctypes.c_double
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp()   # the step appends its proj_mag.dat there
+    h, buf = _ref_handle(lib, fields, nx, ny, nz, prm, outdir=d)
+    try:
+        pm = lib.adv_project(h, dt)
+        lib.adv_get(h, buf.ctypes.data_as(vp))
+    finally:
+        lib.adv_free(h)
+        shutil.rmtree(d, ignore_errors=True)
+    return buf, pm
+
+
+def node_velocities(fields, nx, ny, nz):
+    """(npts, 3) node velocities u, v, w of a ghosted Field array, nodes in
+    natural order with nz + 1 node planes (the top plate included)."""
+    g = NGHOST
+    A = fields.reshape(nz + 2 * g, ny + 2 * g, nx + 2 * g, NFIELD)
+    return np.ascontiguousarray(A[g:g + nz + 1, g:g + ny, g:g + nx, U:W + 1]).reshape(-1, 3)
+
+
+def cell_stresses(fields, nx, ny, nz):
+    """(nz, ny, nx, 6) cell stresses s11 s12 s13 s22 s23 s33 of a ghosted Field array."""
+    return np.ascontiguousarray(interior(fields, nx, ny, nz)[..., S11:S33 + 1])

@@ -100,6 +100,8 @@ int MPI_Cart_coords(MPI_Comm, int, int maxdims, int *coords) {
 
 int MPI_Isend(const void *buf, int count, MPI_Datatype type, int dest, int tag, MPI_Comm,
               MPI_Request *req) {
+    if (req) *req = 0;
+    if (dest == MPI_PROC_NULL) return MPI_SUCCESS;   // no neighbour (a non-periodic edge): nothing moves
     if (dest != 0) throw std::runtime_error("mpi shim: send to a rank other than 0");
     size_t bytes = (size_t)count * type_size(type);
     if (req) *req = 0;
@@ -120,6 +122,8 @@ int MPI_Isend(const void *buf, int count, MPI_Datatype type, int dest, int tag, 
 
 int MPI_Irecv(void *buf, int count, MPI_Datatype type, int src, int tag, MPI_Comm,
               MPI_Request *req) {
+    if (req) *req = 0;
+    if (src == MPI_PROC_NULL) return MPI_SUCCESS;   // no neighbour: the buffer is left as it is
     if (src != 0) throw std::runtime_error("mpi shim: receive from a rank other than 0");
     size_t bytes = (size_t)count * type_size(type);
     if (req) *req = 0;
@@ -141,6 +145,7 @@ int MPI_Send(const void *buf, int count, MPI_Datatype type, int dest, int tag, M
 
 int MPI_Recv(void *buf, int count, MPI_Datatype type, int src, int tag, MPI_Comm comm,
              MPI_Status *) {
+    if (src == MPI_PROC_NULL) return MPI_SUCCESS;
     MPI_Irecv(buf, count, type, src, tag, comm, nullptr);
     if (!g_recvs.empty() && g_recvs.back().buf == buf)
         throw std::runtime_error("mpi shim: blocking receive with no matching send");

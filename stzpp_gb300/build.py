@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libstz_mg.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["api.cu", "smooth.cu", "transfer.cu", "rat.cu", "field.cu", "tail.cu", "noalloc.cu", "adjoint.cu", "tile.cu", "advect.cu", "output.cu", "residual_df.cu"]
+SOURCES = ["api.cu", "smooth.cu", "transfer.cu", "rat.cu", "field.cu", "tail.cu", "noalloc.cu", "adjoint.cu", "tile.cu", "advect.cu", "output.cu", "residual_df.cu", "band.cu"]
 
 
 def nvcc() -> str:

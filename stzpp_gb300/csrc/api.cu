@@ -184,6 +184,15 @@ void sync(stz_mg_handle h) {
     check_launch();
 }
 
+// The band sweep's CTAs give up (and record it) when their staged copies do
+// not arrive in time; a solve or sweep that saw that fails.
+void check_band(stz_mg_handle h) {
+    const int e = band_take_error(h->st);
+    if (e < 0) fail(STZ_MG_ERR_CUDA, "cannot read the band sweep's record");
+    if (e == 2) fail(STZ_MG_ERR_CUDA, "band sweep: shared memory not 128-byte aligned");
+    if (e > 0) fail(STZ_MG_ERR_CUDA, "band sweep: staged copies did not arrive within 0.2 s");
+}
+
 double *staging(stz_mg_handle h, size_t n) {
     if (h->stage_len < n) {
         h->release(h->stage);
@@ -890,6 +899,7 @@ void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double 
             k = std::max(1, std::min(k, 12));
         }
     }
+    check_band(h);
     if (cycles_out) *cycles_out = cycles;
     double rel = std::sqrt(rsq) / (bn > 0 ? bn : 1.0);
     if (relres_out) *relres_out = rel;
@@ -1159,6 +1169,7 @@ int stz_mg_vcycle(stz_mg_handle h) {
             mixed_step(h, 1);
         }
         sync(h);
+        check_band(h);
     });
 }
 
@@ -1385,6 +1396,7 @@ int stz_mg_level_gauss_seidel(stz_mg_handle h, int level, int sweeps) {
         launch_gs_sweeps<double>(h->op64[level], h->geo[level], h->L64[level].r, h->L64[level].x, h->L64[level].res,
                                  sweeps, h->st);
         sync(h);
+        check_band(h);
     });
 }
 
@@ -1464,6 +1476,19 @@ int stz_mg_output_slice(stz_mg_handle h, int which, int k, double ax, double bx,
         sync(h);
         if (!write_slice_file(vals.data(), g.m, g.n, ax, bx, ay, by, filename))
             fail(STZ_MG_ERR_ARG, "stz_mg_output_slice: cannot write %s", filename);
+    });
+}
+
+int stz_mg_sweep_kind(stz_mg_handle h, int level, int *kind, int *launches_per_sweep) {
+    if (!h || !kind) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        const bool mixed = h->d.precision == STZ_MG_MIXED;
+        *kind = mixed ? gs_sweep_kind<float>(h->op32[level], g, h->L32[level].x, true)
+                      : gs_sweep_kind<double>(h->op64[level], g, h->L64[level].x, true);
+        if (launches_per_sweep) *launches_per_sweep = *kind == 0 ? 8 : 2;
     });
 }
 
@@ -1549,6 +1574,7 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
         for (int r = 0; r < reps; r++) launch();
         CK(cudaEventRecord(e1, h->st));
         sync(h);
+        check_band(h);
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);

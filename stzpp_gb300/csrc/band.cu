@@ -1,0 +1,509 @@
+// Band Gauss-Seidel sweep of the fine level: the 8-colour sweep of a shared
+// elasticity stencil on a level periodic in x and y, two launches per sweep,
+// every CTA staging its planes with the tensor-memory-access (TMA) engine.
+//
+// Replaces, for the top level of the shared-stencil problems, the eight
+// colour launches of smooth.cu (region::gauss_seidel, region.cc:1557-1762,
+// in the 8-colour order q = (i&1) + 2(j&1) + 4(k&1)).  Colours 0-3 live on
+// even z-planes and 4-7 on odd ones, and a colour couples only to its own
+// plane and the planes above and below.  So a sweep is two launches (even
+// planes, then odd planes) reading x_in and writing x_out; each CTA takes one
+// band of 8 node rows spanning the whole periodic x range of one plane and
+// runs the plane's four colours in order from shared memory:
+//
+//  * the in-plane chain of the colour order needs only one row of halo: the
+//    colours (a, b) = (0,0), (1,0), (0,1), (1,1) depend on each other
+//    through x-faces (0->1, 2->3), y-faces (0->2, 1->3) and xy-edges (0->3,
+//    1->2), so colours 0 and 1 are computed on the band plus the first row of
+//    the next band, colours 2 and 3 on the band itself, from old values on
+//    the band widened by one row on each side;
+//  * the whole x range is in the CTA, so the periodic wrap in x is an index
+//    wrap in shared memory and there is no x halo at all;
+//  * planes k-1, k, k+1 of the widened band (3 components each) arrive by
+//    cp.async.bulk.tensor boxes completing on one mbarrier; at the periodic
+//    wrap in y a box is split in two (rows N2-1 and 0.. or ..N2-1 and 0);
+//  * the planes above and below are old (x_in, even launch) or new (x_out,
+//    odd launch) values, as in the colour order.
+//
+// Each node update has the arithmetic of const_row (ops.cuh) in the same
+// order, so the sweep is bit-identical to the eight colour launches.  Every
+// wait is an mbarrier wait with a time limit; a CTA whose copies do not
+// arrive in time records the fact (band_take_error) and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+
+#include "launch.h"
+#include "ops.cuh"
+
+namespace stzmg {
+
+__device__ int g_band_err = 0;
+
+namespace {
+
+constexpr int kBandRows = 8;               // node rows of a band
+constexpr int kOwnSub = kBandRows / 2;     // sub-grid rows per parity owned by a band
+constexpr int kStageRows = kOwnSub + 2;    // staged sub-rows J0-1 .. J0+kOwnSub
+
+// Shared-memory layout of the staged band: plane p (0: k-1, 1: k, 2: k+1),
+// component c, sub-row Jr (staged row 0 is sub-row J0-1), colour ab = a + 2b
+// of the plane, sub-grid column I.  JOUT: Jr outside ab (one TMA box per
+// plane and component); otherwise ab outside Jr (one box per colour).
+template <int M2, bool JOUT>
+__host__ __device__ constexpr int woff(int p, int c, int Jr, int ab, int I) {
+    return JOUT ? (((p * 3 + c) * kStageRows + Jr) * 4 + ab) * M2 + I
+                : (((p * 3 + c) * 4 + ab) * kStageRows + Jr) * M2 + I;
+}
+template <int M2>
+constexpr int kBandWords = 3 * 3 * kStageRows * 4 * M2;
+
+template <int B, int E, typename F>
+__device__ __forceinline__ void sfor(F &&f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        sfor<B + 1, E>(f);
+    }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned phase) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for phase `phase` of the barrier for at most `limit_ns`.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned phase, unsigned long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try(bar, phase))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+// One box of a 5-d tensor map into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load5(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                          int c4, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+        : "memory");
+}
+
+// The tensor maps of one field (x_in or x_out): boxes of 6, 5 and 1 sub-rows.
+struct BandMaps {
+    CUtensorMap rows6, rows5, rows1;
+};
+
+struct BandArgs {
+    Geom g;
+    int c;          // plane parity of this launch
+    int nbands;     // n / kBandRows
+};
+
+// Stage plane kk of a field (three components) into buffer plane p: boxes
+// cover sub-rows J0-1 .. J0+kOwnSub, split where they cross the periodic
+// wrap in y.  Every plane delivers a third of kBandWords<M2> elements.
+template <typename T, int M2, bool JOUT>
+__device__ __forceinline__ void stage_plane(const BandMaps &mp, const Geom &g, int kk, int J0, int p,
+                                                unsigned sbase, unsigned bar) {
+    const int K = kk >> 1, cpar = kk & 1;
+    constexpr unsigned rowb = (JOUT ? 4 * M2 : M2) * sizeof(T);   // bytes per staged sub-row of one box
+    const int nab = JOUT ? 1 : 4;
+    for (int comp = 0; comp < 3; comp++)
+        for (int ab = 0; ab < nab; ab++) {
+            const unsigned dst = sbase + (unsigned)(woff<M2, JOUT>(p, comp, 0, ab, 0) * (int)sizeof(T));
+            const int cc = 2 * comp + cpar;
+            // coordinates: JOUT (I, ab, J, K, cc), else (I, J, K, ab, cc)
+            auto load = [&](const CUtensorMap *map, int J, unsigned d) {
+                if (JOUT) tma_load5(d, map, 0, 0, J, K, cc, bar);
+                else tma_load5(d, map, 0, J, K, ab, cc, bar);
+            };
+            if (J0 == 0) {   // rows N2-1 | 0 .. kOwnSub
+                load(&mp.rows1, g.N2 - 1, dst);
+                load(&mp.rows5, 0, dst + rowb);
+            } else if (J0 + kOwnSub == g.N2) {   // rows J0-1 .. N2-1 | 0
+                load(&mp.rows5, J0 - 1, dst);
+                load(&mp.rows1, 0, dst + 5 * rowb);
+            } else {
+                load(&mp.rows6, J0 - 1, dst);
+            }
+        }
+}
+
+// One colour (A, B) of plane k (buffer plane 1) on NR sub-rows J0 .. J0+NR-1
+// of this thread's sub-grid column I: new values from r (rr) and the staged
+// neighbours, in the arithmetic and order of const_row<T, true, false>, then
+// the centre solve.  Neighbour (dx, dy, dz) of a node of parity (A, B) lies in
+// colour ((A+dx)&1, (B+dy)&1) at column I + floor((A+dx)/2) (wrapped: base
+// index ib[0..2] for shifts -1, 0, +1) and staged row Jr + floor((B+dy)/2).
+template <typename T, int M2, bool JOUT, int A, int B, int NR>
+__device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (&ib)[3], const ConstOp<T> &op,
+                                            const T (&rr)[NR][3], T (&out)[NR][3]) {
+#pragma unroll
+    for (int t = 0; t < NR; t++) {
+        const int Jr = t + 1;
+        T v[27][3];
+        sfor<0, 27>([&](auto bi) {
+            constexpr int b = decltype(bi)::value;
+            if constexpr (b != 13 && nnz_axes(b) != 3) {
+                constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+                constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+                constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+                sfor<0, 3>([&](auto ci) {
+                    constexpr int c = decltype(ci)::value;
+                    constexpr bool used = elastic_entry(b, c) || elastic_entry(b, 3 + c) || elastic_entry(b, 6 + c);
+                    if constexpr (used) v[b][c] = s[ib[sI + 1] + woff<M2, JOUT>(1 + dz, c, 0, ap + 2 * bp, 0) +
+                                                    (Jr + sJ) * woff<M2, JOUT>(0, 0, 1, 0, 0)];
+                    else v[b][c] = T(0);
+                });
+            }
+        });
+        T acc[3] = {rr[t][0], rr[t][1], rr[t][2]};
+#pragma unroll
+        for (int b = 0; b < 27; b++) {
+            if (b == 13 || nnz_axes(b) == 3) continue;
+#pragma unroll
+            for (int e = 0; e < 9; e++)
+                if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[b][e % 3];
+        }
+        const T *inv = op.inv_int;
+        out[t][0] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+        out[t][1] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+        out[t][2] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
+    }
+}
+
+// Slot (component 0) of colour ab of plane parity c, sub-grid row J (wrapped), column I.
+__device__ __forceinline__ size_t band_slot(const Geom &g, int ab, int c, int K, int J, int I) {
+    return (size_t)(ab + 4 * c) * g.S + ((size_t)K * g.N2 + J) * g.M2 + I;
+}
+
+template <typename T, int M2, bool JOUT>
+__global__ void __launch_bounds__(M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
+    gs_band_kernel(const BandArgs args, const __grid_constant__ ConstOp<T> op, const __grid_constant__ BandMaps in,
+                   const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
+    extern __shared__ __align__(128) unsigned char band_smem[];
+    __shared__ __align__(8) unsigned long long bar_store;
+    const Geom &g = args.g;
+    const int I = threadIdx.x;
+    const int band = blockIdx.x % args.nbands, kidx = blockIdx.x / args.nbands;
+    const int c = args.c, k = 2 * kidx + c, K = kidx;
+    const int J0 = band * kOwnSub;
+    const size_t np = (size_t)g.npad;
+    const bool zin = g.zp || (k != 0 && k != g.o - 1);
+
+    if (!zin) {   // a Dirichlet plate: x = fix^-1 r, no neighbours
+        const T *inv = op.inv_fix;
+#pragma unroll 1
+        for (int ab = 0; ab < 4; ab++)
+#pragma unroll 1
+            for (int t = 0; t < kOwnSub; t++) {
+                const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
+                const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
+                xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
+                xout[sl + np] = dot3(inv[3], a0, inv[4], a1, inv[5], a2);
+                xout[sl + 2 * np] = dot3(inv[6], a0, inv[7], a1, inv[8], a2);
+            }
+        return;
+    }
+
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&bar_store);
+    if (I == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // TMA boxes land at 128-byte aligned shared addresses only
+    const bool aligned = (sbase & 127u) == 0;
+    if (I == 0 && aligned) {
+        // every box of the three planes, announced before any is issued
+        mbar_expect_tx(bar, (unsigned)(kBandWords<M2> * sizeof(T)));
+        // the z-neighbour planes: old values (x_in) under the even launch,
+        // new ones (x_out) under the odd launch; plane k itself from x_in
+        const BandMaps &zm = c == 0 ? in : out_maps;
+        const int klo = k == 0 ? g.o - 1 : k - 1, khi = k == g.o - 1 ? 0 : k + 1;
+        stage_plane<T, M2, JOUT>(zm, g, klo, J0, 0, sbase, bar);
+        stage_plane<T, M2, JOUT>(in, g, k, J0, 1, sbase, bar);
+        stage_plane<T, M2, JOUT>(zm, g, khi, J0, 2, sbase, bar);
+    }
+    if (!aligned) {
+        if (I == 0) atomicExch(&g_band_err, 2);
+        return;
+    }
+    // r of every node this thread updates, while the boxes are in flight
+    T r0[kOwnSub + 1][3], r1[kOwnSub + 1][3], r2[kOwnSub][3], r3[kOwnSub][3];
+#pragma unroll
+    for (int t = 0; t <= kOwnSub; t++) {
+        const int J = J0 + t == g.N2 ? 0 : J0 + t;
+        const size_t s0 = band_slot(g, 0, c, K, J, I), s1 = band_slot(g, 1, c, K, J, I);
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            r0[t][cc] = r[s0 + cc * np];
+            r1[t][cc] = r[s1 + cc * np];
+        }
+        if (t < kOwnSub) {
+            const size_t s2 = band_slot(g, 2, c, K, J, I), s3 = band_slot(g, 3, c, K, J, I);
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                r2[t][cc] = r[s2 + cc * np];
+                r3[t][cc] = r[s3 + cc * np];
+            }
+        }
+    }
+    const bool ok = mbar_wait(bar, 0, 200000000ull);   // 0.2 s: copies that never arrive
+    if (!__syncthreads_and(ok)) {
+        if (I == 0) {
+            atomicExch(&g_band_err, 1);
+            mbar_wait(bar, 0, 200000000ull);   // let copies still in flight land before the CTA leaves
+        }
+        __syncthreads();
+        return;
+    }
+
+    T *s = reinterpret_cast<T *>(band_smem);
+    const int ib[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
+    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    // store a colour's new values: shared memory for the later colours, x_out
+    // for the rows this band owns
+    auto emit = [&](auto A_, auto B_, auto NR_, const auto &o, bool to_smem) {
+        constexpr int A = decltype(A_)::value, B = decltype(B_)::value, NR = decltype(NR_)::value;
+#pragma unroll
+        for (int t = 0; t < NR; t++) {
+            if (to_smem)
+#pragma unroll
+                for (int cc = 0; cc < 3; cc++) s[I + woff<M2, JOUT>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[t][cc];
+            if (t < kOwnSub) {
+                const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
+#pragma unroll
+                for (int cc = 0; cc < 3; cc++) xout[sl + cc * np] = o[t][cc];
+            }
+        }
+    };
+    using I0 = std::integral_constant<int, 0>;
+    using I1 = std::integral_constant<int, 1>;
+    using NRb0 = std::integral_constant<int, kOwnSub + 1>;
+    using NRb1 = std::integral_constant<int, kOwnSub>;
+    {
+        T o[kOwnSub + 1][3];
+        band_colour<T, M2, JOUT, 0, 0, kOwnSub + 1>(s, ib, op, r0, o);
+        emit(I0{}, I0{}, NRb0{}, o, true);
+    }
+    __syncthreads();
+    {
+        T o[kOwnSub + 1][3];
+        band_colour<T, M2, JOUT, 1, 0, kOwnSub + 1>(s, ib, op, r1, o);
+        emit(I1{}, I0{}, NRb0{}, o, true);
+    }
+    __syncthreads();
+    {
+        T o[kOwnSub][3];
+        band_colour<T, M2, JOUT, 0, 1, kOwnSub>(s, ib, op, r2, o);
+        emit(I0{}, I1{}, NRb1{}, o, true);
+    }
+    __syncthreads();
+    {
+        T o[kOwnSub][3];
+        band_colour<T, M2, JOUT, 1, 1, kOwnSub>(s, ib, op, r3, o);
+        emit(I1{}, I1{}, NRb1{}, o, false);
+    }
+}
+
+// ------------------------------------------------------------------ host
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// The tensor maps of one colour-blocked field of level g: a 5-d view with
+// column I innermost, then (JOUT) colour ab, sub-row J, plane K, component x
+// plane parity -- or (not JOUT) J, K, ab -- and boxes of the whole row of M2
+// columns, 4 colours (JOUT) or one, and 6, 5 or 1 sub-rows.
+template <typename T, bool JOUT>
+bool make_band_maps(const Geom &g, const T *field, BandMaps &mp) {
+    EncodeTiled enc = encoder();
+    if (!enc) return false;
+    const cuuint64_t e = sizeof(T);
+    const cuuint64_t M2 = g.M2, N2 = g.N2, O2 = g.O2, S = g.S;
+    cuuint64_t dims[5], strides[4];
+    if (JOUT) {
+        const cuuint64_t d[5] = {M2, 4, N2, O2, 6}, st[4] = {S * e, M2 * e, M2 * N2 * e, 4 * S * e};
+        std::memcpy(dims, d, sizeof d);
+        std::memcpy(strides, st, sizeof st);
+    } else {
+        const cuuint64_t d[5] = {M2, N2, O2, 4, 6}, st[4] = {M2 * e, M2 * N2 * e, S * e, 4 * S * e};
+        std::memcpy(dims, d, sizeof d);
+        std::memcpy(strides, st, sizeof st);
+    }
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    CUtensorMap *maps[3] = {&mp.rows6, &mp.rows5, &mp.rows1};
+    const cuuint32_t rows[3] = {kStageRows, kStageRows - 1, 1};
+    for (int i = 0; i < 3; i++) {
+        cuuint32_t box[5];
+        if (JOUT) {
+            const cuuint32_t b[5] = {(cuuint32_t)M2, 4, rows[i], 1, 1};
+            std::memcpy(box, b, sizeof b);
+        } else {
+            const cuuint32_t b[5] = {(cuuint32_t)M2, rows[i], 1, 1, 1};
+            std::memcpy(box, b, sizeof b);
+        }
+        if (enc(maps[i], dt, 5, const_cast<T *>(field), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
+}
+
+// Layout of the tensor maps the driver accepts: 1 the colour-inner view (one
+// box per plane and component), 0 the monotonic view (one box per colour),
+// -1 neither (the colour launches run instead).  Decided once per process.
+template <typename T>
+int band_layout(const Geom &g, const T *field) {
+    static int layout = -2;
+    if (layout == -2) {
+        BandMaps mp;
+        if (make_band_maps<T, true>(g, field, mp)) layout = 1;
+        else if (make_band_maps<T, false>(g, field, mp)) layout = 0;
+        else layout = -1;
+    }
+    return layout;
+}
+
+bool first_band_use(unsigned long long &devices) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (devices & bit) return false;
+    devices |= bit;
+    return true;
+}
+
+template <typename T, int M2, bool JOUT>
+bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+    BandMaps min_, mout;
+    if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
+    auto kern = gs_band_kernel<T, M2, JOUT>;
+    const int smem = kBandWords<M2> * (int)sizeof(T);
+    static unsigned long long attr_devices = 0;
+    if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    BandArgs a;
+    a.g = g;
+    a.nbands = g.n / kBandRows;
+    for (int c = 0; c < 2; c++) {
+        const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
+        if (planes <= 0) continue;
+        a.c = c;
+        kern<<<a.nbands * planes, M2, smem, st>>>(a, op.cop, min_, mout, r, xout);
+    }
+    return true;
+}
+
+template <typename T, bool JOUT>
+bool launch_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+    switch (g.M2) {
+        case 32: return launch_band_k<T, 32, JOUT>(op, g, r, xin, xout, st);
+        case 64: return launch_band_k<T, 64, JOUT>(op, g, r, xin, xout, st);
+        case 128: return launch_band_k<T, 128, JOUT>(op, g, r, xin, xout, st);
+        default: return false;
+    }
+}
+
+}  // namespace
+
+// Where the band sweep runs: the elasticity stencil shared by every interior
+// node, a level periodic in x and y with an even number of columns in 32,
+// 64 or 128 sub-grid columns (64 .. 256 nodes) and whole bands of 8 rows (at
+// least two), an even z extent if z is periodic.  FP32 levels by default;
+// STZ_MG_BAND=0 turns it off, STZ_MG_BAND=1 uses it in FP64 too.
+template <typename T>
+bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
+    int mode = -1;
+    if (const char *e = std::getenv("STZ_MG_BAND")) mode = std::atoi(e) != 0;
+    if (mode == 0) return false;
+    if (mode < 0 && sizeof(T) != 4) return false;
+    if (op.kind != OP_CONST || !op.cop.elastic) return false;
+    if (!g.xp || !g.yp || (g.m & 1) || g.n % kBandRows != 0 || g.n < 2 * kBandRows) return false;
+    if (g.M2 != 32 && g.M2 != 64 && g.M2 != 128) return false;
+    if (g.zp && (g.o & 1)) return false;
+    return true;
+}
+
+// One sweep x_in -> x_out; false when the tensor maps cannot be made (the
+// caller then sweeps with the colour launches).
+template <typename T>
+bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+    const int layout = band_layout<T>(g, xin);
+    if (layout == 1) return launch_band_m<T, true>(op, g, r, xin, xout, st);
+    if (layout == 0) return launch_band_m<T, false>(op, g, r, xin, xout, st);
+    return false;
+}
+
+// Whether the tensor maps of the band sweep can be made for this level.
+template <typename T>
+bool gs_band_ready(const Geom &g, const T *field) {
+    return band_layout<T>(g, field) >= 0;
+}
+template bool gs_band_ready<float>(const Geom &, const float *);
+template bool gs_band_ready<double>(const Geom &, const double *);
+
+// 1 if a band CTA gave up waiting for its copies since the last call, 2 if
+// one found its shared memory misaligned for TMA (and clears the record);
+// -1 if the record cannot be read.
+int band_take_error(cudaStream_t st) {
+    int v = 0, z = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_band_err, sizeof v, 0, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+    if (cudaMemcpyToSymbolAsync(g_band_err, &z, sizeof z, 0, cudaMemcpyHostToDevice, st) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    return v;
+}
+
+template bool gs_band_applies<float>(const LevelOp<float> &, const Geom &);
+template bool gs_band_applies<double>(const LevelOp<double> &, const Geom &);
+template bool launch_gs_sweep_band<float>(const LevelOp<float> &, const Geom &, const float *, const float *, float *,
+                                          cudaStream_t);
+template bool launch_gs_sweep_band<double>(const LevelOp<double> &, const Geom &, const double *, const double *,
+                                           double *, cudaStream_t);
+
+}  // namespace stzmg

@@ -34,6 +34,24 @@ template <typename T>
 bool gs_tile_applies(const LevelOp<T> &op, const Geom &g);
 template <typename T>
 void launch_gs_sweep_tile(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st);
+// band.cu: one sweep reading xin and writing xout on the top level of a
+// shared elasticity stencil periodic in x, y (full-width bands of 8 rows,
+// planes staged by TMA); false if the tensor maps cannot be made
+template <typename T>
+bool gs_band_applies(const LevelOp<T> &op, const Geom &g);
+template <typename T>
+bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st);
+template <typename T>
+bool gs_band_ready(const Geom &g, const T *field);
+// How launch_gs_sweeps smooths a level: 0 eight colour launches per sweep,
+// 1 the tiled two-buffer sweep, 2 the band sweep, 3 the plane-phase kernels
+// (two launches per sweep each but the first)
+template <typename T>
+int gs_sweep_kind(const LevelOp<T> &op, const Geom &g, const T *x, bool has_tmp);
+// 1 if a band CTA gave up waiting for its copies since the last call, 2 if
+// one found its shared memory misaligned for TMA (the record is cleared),
+// 0 if none did, -1 if the record cannot be read
+int band_take_error(cudaStream_t st);
 // tile.cu: res = r - A x by plane tiles staged in shared memory; with
 // partial non-null, per-CTA sums of |res|^2
 template <typename T>

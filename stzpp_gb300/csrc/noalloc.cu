@@ -46,7 +46,10 @@ double *g_addr[kMaxDevices] = {};
 
 // Device address of the scratch, looked up once per device with that device
 // current (the lookup may load the module on the device, so the first call on
-// a device is made before the caller starts any stream capture).
+// a device is made before the caller starts any stream capture).  The address
+// stays valid while the device's primary context lives: a cudaDeviceReset
+// between calls would leave it stale, and callers do not reset the device
+// between calls.
 cudaError_t scratch_address(int device, double **out) {
     std::lock_guard<std::mutex> lock(g_addr_mutex);
     if (!g_addr[device]) {
@@ -176,6 +179,16 @@ extern "C" int stz_mg_const_residual_sumsq_noalloc(int m, int n, int o, int x_pr
     if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     int rc = STZ_MG_OK;
     double *partial = nullptr;
+    if (stream) {   // the stream must belong to `device`
+        int sdev = -1;
+        e = cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamGetDevice");
+        else if (sdev != device) rc = stzmg::record_error(STZ_MG_ERR_ARG, "stream belongs to another device");
+        if (rc != STZ_MG_OK) {
+            if (prev != device && prev >= 0) cudaSetDevice(prev);
+            return rc;
+        }
+    }
     e = scratch_address(device, &partial);
     if (e != cudaSuccess) {
         rc = cuda_fail(e, "cudaGetSymbolAddress");
@@ -185,6 +198,7 @@ extern "C" int stz_mg_const_residual_sumsq_noalloc(int m, int n, int o, int x_pr
         for (int q = 0; q < 9; q++) A.f[q] = fix[q];
         const int nblocks = (int)((npts + kNodesPerBlock - 1) / kNodesPerBlock);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        cudaGetLastError();   // an earlier caller's launch error is not this call's
         const_residual_sumsq_kernel<<<nblocks, kThreads, 0, st>>>(A, m, n, o, x_prd != 0, y_prd != 0, z_prd != 0, x,
                                                                    b, partial);
         sum_noalloc_partials_kernel<<<1, 1024, 0, st>>>(partial, nblocks, sumsq);

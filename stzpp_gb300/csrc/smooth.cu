@@ -340,12 +340,28 @@ void launch_gs_sweeps(const LevelOp<T> &op, const Geom &g, const T *r, T *x, T *
     // plane-invariant levels of 64x64 and more: 4+ tiles per plane beat one
     // block per plane (64x64x65, two FP32 sweeps: 58 vs 107 us); 32x32 does not
     const bool plane_tiles = op.kind == OP_PLANE && g.m * g.n >= 64 * 64;
+    // the fine level of a shared elasticity stencil: full-width bands whose
+    // planes arrive by TMA (band.cu)
+    if (tmp && gs_band_applies(op, g)) {
+        for (; s + 2 <= sweeps; s += 2) {
+            if (!launch_gs_sweep_band(op, g, r, x, tmp, st)) break;
+            launch_gs_sweep_band(op, g, r, tmp, x, st);
+        }
+    }
     if (tmp && (large_planes<T>(g) || plane_tiles) && gs_tile_applies(op, g))
         for (; s + 2 <= sweeps; s += 2) {
             launch_gs_sweep_tile(op, g, r, x, tmp, st);
             launch_gs_sweep_tile(op, g, r, tmp, x, st);
         }
     for (; s < sweeps; s++) launch_gs_sweep(op, g, r, x, st);
+}
+
+template <typename T>
+int gs_sweep_kind(const LevelOp<T> &op, const Geom &g, const T *x, bool has_tmp) {
+    const bool plane_tiles = op.kind == OP_PLANE && g.m * g.n >= 64 * 64;
+    if (has_tmp && gs_band_applies(op, g) && gs_band_ready(g, x)) return 2;
+    if (has_tmp && (large_planes<T>(g) || plane_tiles) && gs_tile_applies(op, g)) return 1;
+    return large_planes<T>(g) ? 0 : 3;
 }
 
 template <typename T>
@@ -408,6 +424,8 @@ void launch_residual(const LevelOp<T> &op, const Geom &g, const T *r, const T *x
 
 template void launch_gs_colour<float>(const LevelOp<float> &, const Geom &, int, const float *, float *, cudaStream_t);
 template void launch_gs_colour<double>(const LevelOp<double> &, const Geom &, int, const double *, double *, cudaStream_t);
+template int gs_sweep_kind<float>(const LevelOp<float> &, const Geom &, const float *, bool);
+template int gs_sweep_kind<double>(const LevelOp<double> &, const Geom &, const double *, bool);
 template void launch_gs_sweep<float>(const LevelOp<float> &, const Geom &, const float *, float *, cudaStream_t);
 template void launch_gs_sweep<double>(const LevelOp<double> &, const Geom &, const double *, double *, cudaStream_t);
 template void launch_gs_sweeps<float>(const LevelOp<float> &, const Geom &, const float *, float *, float *, int,

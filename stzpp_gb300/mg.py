@@ -39,7 +39,7 @@ EXPORTS = (
     "stz_mg_solve_stats", "stz_mg_residual_norm", "stz_mg_l2_error_all", "stz_mg_num_levels", "stz_mg_level_dims",
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
-    "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_const_residual_sumsq_noalloc",
+    "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_sweep_kind", "stz_mg_const_residual_sumsq_noalloc",
     "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update", "stz_mg_advection_step",
     "stz_mg_output_slice", "stz_mg_cube_values", "stz_mg_output_cube",
 )
@@ -101,6 +101,7 @@ def load_library():
     lib.stz_mg_level_interpolation.argtypes = [vp, ci]
     lib.stz_mg_level_residual.argtypes = [vp, ci, vp, ctypes.POINTER(cd), ci]
     lib.stz_mg_time_kernel.argtypes = [vp, ci, ci, ci, ctypes.POINTER(cd), ctypes.POINTER(cd)]
+    lib.stz_mg_sweep_kind.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
     lib.stz_mg_const_residual_sumsq_noalloc.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, ci, vp]
     lib.stz_mg_adjoint_solve.argtypes = [vp, vp, vp, ci, cd, ci, ctypes.POINTER(ci), ctypes.POINTER(cd)]
     lib.stz_mg_coeff_grad.argtypes = [vp, vp, vp, vp, vp, ci]
@@ -445,6 +446,13 @@ class Multigrid:
         ax, bx, ay, by = box if box is not None else (0.0, m - 1.0, 0.0, n - 1.0)
         code = {"x": 0, "r": 1, "residual": 2}[which]
         _check(load_library().stz_mg_output_slice(self._h, code, k, ax, bx, ay, by, os.fsencode(filename)))
+
+    def sweep_kind(self, level=0):
+        """(kind, launches per sweep) of the smoother of a level: kind is one
+        of "colour", "tile", "band", "phase"."""
+        k, n = ctypes.c_int(), ctypes.c_int()
+        _check(load_library().stz_mg_sweep_kind(self._h, level, ctypes.byref(k), ctypes.byref(n)))
+        return ("colour", "tile", "band", "phase")[k.value], n.value
 
     def time_kernel(self, kernel, level=0, reps=20):
         """(ms per launch, algorithmic bytes or FP64 flops per launch) of one

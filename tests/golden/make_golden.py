@@ -33,7 +33,11 @@ Field member of shear_sim_3d::output_cube on a seeded 6x5x4 grid, and the
 x, r and residual z-slices of region::output_internal on an 8x6x5 multigrid
 level -> tests/golden/output_files.npz (inputs and file bytes).
 
-Run: python tests/golden/make_golden.py [trans | adv | out]
+Also ``proj``: the reference's r_field and its whole quasi-static projection
+step (shear_sim_3d::projection_step: multigrid solve, stress update,
+proj_mag) through oracle/_ref/libstzadv.so -> tests/golden/proj_step.npz.
+
+Run: python tests/golden/make_golden.py [trans | adv | out | proj]
 """
 import os
 import sys
@@ -144,6 +148,36 @@ def adv_steps(path):
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+# (name, cells nx ny nz, seed, dt, stress scale): quasi-static projection steps
+PROJ_CASES = [("a", (8, 6, 5), 4, 0.002, 0.5), ("b", (12, 10, 8), 7, 0.01, 0.2)]
+
+
+def projection_steps(path):
+    """The reference's r_field of every node and its whole projection step
+    (multigrid solve, stress update, proj_mag) on seeded ghosted grids, x and
+    y periodic with z plates: inputs (cell stresses), and outputs (node
+    right-hand side, solved node velocities, new cell stresses, proj_mag)."""
+    from oracle import advect as A
+    if not A.reference_available():
+        sys.exit("oracle/_ref/libstzadv.so is missing: run `make -C oracle advref` where the reference is available")
+    out = {}
+    for name, (nx, ny, nz), seed, dt, scale in PROJ_CASES:
+        prm = A.driver_params(nx)
+        F = A.random_fields(seed, nx, ny, nz, sigma_scale=scale)
+        r = A.reference_rhs(F, nx, ny, nz, prm)
+        G, pm = A.reference_projection(F, nx, ny, nz, prm, dt)
+        out[name + "/cells"] = np.array([nx, ny, nz])
+        out[name + "/dt"] = np.float64(dt)
+        out[name + "/lamb_mu"] = np.array([prm["lamb"], prm["mu"]])
+        out[name + "/sigma"] = A.cell_stresses(F, nx, ny, nz)
+        out[name + "/rhs"] = r
+        out[name + "/u"] = A.node_velocities(G, nx, ny, nz)
+        out[name + "/sigma_new"] = A.cell_stresses(G, nx, ny, nz)
+        out[name + "/proj_mag"] = np.float64(pm)
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 OUT_CUBE = (6, 5, 4)
 OUT_SLICE = ((8, 6, 5), (True, True, False), 2, [(0.0, 7.0, 0.0, 5.0), (0.0, 1.0, -0.5, 0.5)])
 OUT_COLS = list(range(10)) + [20, 21, 22]   # u v w s11..s33 chi xi_x xi_y xi_z
@@ -185,6 +219,9 @@ def output_files(path):
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "out":
         output_files(os.path.join(HERE, "output_files.npz"))
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "proj":
+        projection_steps(os.path.join(HERE, "proj_step.npz"))
         return
     if len(sys.argv) > 1 and sys.argv[1] == "adv":
         adv_steps(os.path.join(HERE, "adv_step.npz"))

@@ -320,3 +320,83 @@ def test_tiled_sweep_mixed_solve_bitwise(dims, per, kind, monkeypatch):
     assert np.isfinite(out["0"][1]) and out["0"][1] < 1e-3
     assert out["0"][:2] == out["1"][:2]
     assert np.array_equal(out["0"][2], out["1"][2])
+
+
+BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), 2), ((64, 64, 16), (True, True, True), 2),
+                    ((128, 64, 9), (True, True, False), 3), ((128, 128, 8), (True, True, True), 2),
+                    ((256, 256, 9), (True, True, False), 2), ((64, 16, 5), (True, True, False), 4)]
+
+
+@pytest.mark.parametrize("dims,per,sweeps", BAND_LEVEL_CASES)
+def test_band_sweep_is_the_colour_sweep(dims, per, sweeps, monkeypatch):
+    """The band sweep of the fine level (full-width bands of 8 rows, planes
+    staged by TMA boxes, split at the periodic wrap in y) gives bit for bit the
+    result of the eight colour launches: FP64 level sweeps of the elasticity
+    stencil, Dirichlet and periodic z, 32, 64 and 128 sub-grid columns, two
+    bands (both at the wrap) and many, even and odd sweep counts."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    st, fix = sg.elastic_stencil(1.0, 2.0, *P.grid_spacing(m, n, o, per))
+    out = {}
+    for band in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_BAND", band)
+        monkeypatch.setenv("STZ_MG_TILE", "0")
+        with sg.Multigrid(dims, per, precision="fp64", bottom="gs", max_coarse=10 ** 6) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            N = mg.level_npts(0)
+            rng = np.random.default_rng(11)
+            mg.level_set_field(0, "x", rng.standard_normal((N, 3)))
+            mg.level_set_field(0, "r", rng.standard_normal((N, 3)))
+            mg.gauss_seidel(0, sweeps)
+            out[band] = mg.level_get_field(0, "x")
+    assert np.array_equal(out["0"], out["1"])
+
+
+@pytest.mark.parametrize("dims,per", [((128, 128, 33), (True, True, False)), ((256, 256, 17), (True, True, False)),
+                                      ((128, 64, 24), (True, True, False))])
+def test_band_sweep_mixed_solve_bitwise(dims, per, monkeypatch):
+    """The FP32 V-cycles of the mixed solve with the band sweep on the fine
+    level (the default) and with the colour launches give the same cycle
+    count and the same solution bit for bit (an even plane count puts the
+    upper plate on an odd plane)."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per, h=1.0 / m)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    out = {}
+    for band in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_BAND", band)
+        with sg.Multigrid(dims, per, precision="mixed", sweep_growth=False, v_down=2, v_up=3) as mg:
+            mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, *h))
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-10, 8, check=False)
+            out[band] = (cyc, rel, mg.get_x())
+    assert np.isfinite(out["0"][1]) and out["0"][1] < 1e-3
+    assert out["0"][:2] == out["1"][:2]
+    assert np.array_equal(out["0"][2], out["1"][2])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_cluster_tail_is_the_level_graph(precision, monkeypatch):
+    """The persistent cluster kernels for the small levels (STZ_MG_TAIL=1:
+    the down and up halves of the cycle below 300,000 nodes each in one
+    thread-block cluster launch, cluster barriers between phases) give the
+    per-level launches' cycle count and solution bit for bit."""
+    import stzpp_gb300 as sg
+    dims, per = (128, 128, 129), (True, True, False)
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    out = {}
+    for tail in ("0", "1"):
+        if tail == "1":
+            monkeypatch.setenv("STZ_MG_TAIL", "1")
+        else:
+            monkeypatch.delenv("STZ_MG_TAIL", raising=False)
+        with sg.Multigrid(dims, per, precision=precision, sweep_growth=False, v_down=2, v_up=3) as mg:
+            mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, *h))
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-10, 30)
+            out[tail] = (cyc, rel, mg.get_x())
+    assert out["0"][:2] == out["1"][:2]
+    assert np.array_equal(out["0"][2], out["1"][2])

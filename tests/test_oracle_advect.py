@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import advect as A
+from oracle import problem as P
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "adv_step.npz")
 ADV_IN = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 19, 27]
@@ -54,3 +55,45 @@ def test_restatement_matches_live_reference(dims, seed, dt, bias):
     R = A.reference_step(F, nx, ny, nz, prm, dt)
     P, _ = A.port_step(F, nx, ny, nz, prm, dt)
     assert np.array_equal(R, P)
+
+
+# ------------------------------------------- the steps on either side of the solve
+def _proj_cases():
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "proj_step.npz"))
+    for name in ("a", "b"):
+        yield name, {k.split("/", 1)[1]: d[k] for k in d.files if k.startswith(name + "/")}
+
+
+def test_rhs_and_stress_update_restatements_match_the_reference_fixture():
+    """The numpy restatements of r_field (the node divergence of the cell
+    stresses) and of the projection-step stress update equal, bit for bit,
+    the reference's own r_field and projection_step (tests/golden/proj_step.npz,
+    made by tests/golden/make_golden.py proj from the compiled reference)."""
+    for name, c in _proj_cases():
+        nx, ny, nz = (int(v) for v in c["cells"])
+        dims, per = (nx, ny, nz + 1), (True, True, False)
+        h = P.grid_spacing(*dims, per)
+        assert np.array_equal(P.rhs_divergence(c["sigma"], *dims, per, *h), c["rhs"]), name
+        lamb, mu = c["lamb_mu"]
+        new, modsq = P.stress_update(c["u"], c["sigma"], lamb, mu, float(c["dt"]), *h, dims, per)
+        assert np.array_equal(new, c["sigma_new"]), name
+        assert abs(modsq.sum() - float(c["proj_mag"])) <= 1e-13 * float(c["proj_mag"])
+
+
+def test_projection_step_live_against_the_reference():
+    """Where the reference is compiled: its r_field and projection step on a
+    grid the fixture does not hold, against the restatements."""
+    from oracle import advect as A
+    if not A.reference_available():
+        pytest.skip("compiled reference not available on this machine")
+    nx, ny, nz = 10, 8, 6
+    prm = A.driver_params(nx)
+    F = A.random_fields(13, nx, ny, nz, sigma_scale=0.4)
+    dims, per = (nx, ny, nz + 1), (True, True, False)
+    h = P.grid_spacing(*dims, per)
+    sig = A.cell_stresses(F, nx, ny, nz)
+    assert np.array_equal(A.reference_rhs(F, nx, ny, nz, prm), P.rhs_divergence(sig, *dims, per, *h))
+    G, pm = A.reference_projection(F, nx, ny, nz, prm, 0.005)
+    new, modsq = P.stress_update(A.node_velocities(G, nx, ny, nz), sig, prm["lamb"], prm["mu"], 0.005, *h, dims, per)
+    assert np.array_equal(new, A.cell_stresses(G, nx, ny, nz))
+    assert abs(modsq.sum() - pm) <= 1e-13 * pm
