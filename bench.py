@@ -48,13 +48,14 @@ TOL = 1e-10
 WORKLOAD = ("quasi-static projection solve, 256x256x257 nodes (257^3 problem: periodic x,y, Dirichlet z), "
             "mu=1, lambda=2, dx=1/256, RHS = divergence of N(0,1e-3) cell strain (seed 0), x0 = 0, "
             "to relative residual 1e-10")
-# Cycle of the GPU solves: two sweeps down, three up on every level.  Measured
-# at 256x256x257 on a GB300 (mixed / FP64 ms per solve, earlier kernels):
-# V(2,2) 44.2 / 242, V(2,3) 41.8 / 222, V(3,3) 43.5 / 231, V(3,2) 45.1 / 222,
-# V(2,1) 53.9 / 260; with the current kernels V(2,3) 36.7 ms (11 cycles)
-# against the reference's growing schedule (v + i sweeps on level i):
-# V(1,2) 57.2 (20 cycles), V(2,2) 46.0 (14), V(1,3) 46.5 (14), V(1,1) 68.7 (30).
-V_DOWN, V_UP = 2, 3
+# Cycle of the GPU solves: two sweeps down, four up on every level.  Measured
+# at 256x256x257 on a GB300 with the band sweeps (mixed ms per solve, cycles):
+# V(2,4) 24.3 (10), V(2,3) 25.8 (11), V(2,2) 26.6 (14), V(3,3) 30.7 (10),
+# V(4,4) 34.2 (10): pairs of sweeps run as band sweeps, an odd one as eight
+# colour launches, so even counts pay off.  With the colour launches alone
+# (earlier kernels) V(2,3) was best: 41.8 ms against V(2,2) 44.2, V(3,3) 43.5,
+# and the reference's growing schedule (v + i sweeps on level i) V(2,2) 46.0.
+V_DOWN, V_UP = 2, 4
 
 
 def peaks():

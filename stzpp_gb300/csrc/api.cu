@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -102,6 +103,7 @@ struct stz_mg_handle_s {
     // set-up scratch kept between set-ups (a coefficient change re-runs set-up)
     double *bot_aug = nullptr, *bot_col = nullptr, *bot_dense = nullptr;
     int *bot_piv = nullptr, *bot_S = nullptr;
+    bool bottom_fourier = false;   // the bottom inverse came from the Fourier blocks
     size_t bot_aug_len = 0, bot_dense_len = 0, bot_S_len = 0;
     // scratch
     double *partial = nullptr;
@@ -403,6 +405,117 @@ void require_finite(stz_mg_handle h, const double *d, size_t n, const char *what
 }
 
 // ------------------------------------------------------------ setup
+// Inverse of a bottom operator M (nr x nr, natural node order, 3 rows per
+// node) that commutes with the translations of a grid periodic in x and y:
+// M couples column (i, j) to column (i + dx, j + dy) through a block A(d) of
+// (3o x 3o) that does not depend on (i, j), so the discrete Fourier transform
+// in x and y splits M into m n independent complex systems
+//   D(t) = sum_d A(d) e^{i t.d},  t = 2 pi (kx / m, ky / n),
+// and M^-1 couples (i, j) to (i + dx, j + dy) through
+//   B(d) = 1/(m n) sum_t D(t)^-1 e^{-i t.d}.
+// m n inversions of order 3o instead of one of order 3 m n o.  False when M
+// is not exactly invariant (then the general inverse runs); fails if some
+// D(t) is singular.
+bool fourier_bottom_inverse(const Geom &g, const std::vector<double> &M, int nr, std::vector<double> &inv) {
+    using cd = std::complex<double>;
+    const int m = g.m, n = g.n, o = g.o, bs = 3 * o, cols = m * n;
+    if (!g.xp || !g.yp || nr != 3 * cols * o) return false;
+    auto row = [&](int i, int j, int k, int a) { return (size_t)3 * (i + (size_t)m * (j + (size_t)n * k)) + a; };
+    // A(d)[(k,a),(k',c)] from the rows of column (0, 0); every other row must match
+    std::vector<double> A((size_t)cols * bs * bs);
+    for (int dj = 0; dj < n; dj++)
+        for (int di = 0; di < m; di++)
+            for (int k = 0; k < o; k++)
+                for (int a = 0; a < 3; a++)
+                    for (int k2 = 0; k2 < o; k2++)
+                        for (int c = 0; c < 3; c++)
+                            A[((size_t)(di + m * dj) * bs + 3 * k + a) * bs + 3 * k2 + c] =
+                                M[row(0, 0, k, a) * nr + row(di, dj, k2, c)];
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++)
+            for (int k = 0; k < o; k++)
+                for (int a = 0; a < 3; a++) {
+                    const double *r = &M[row(i, j, k, a) * nr];
+                    for (int dj = 0; dj < n; dj++)
+                        for (int di = 0; di < m; di++)
+                            for (int k2 = 0; k2 < o; k2++)
+                                for (int c = 0; c < 3; c++)
+                                    if (r[row((i + di) % m, (j + dj) % n, k2, c)] !=
+                                        A[((size_t)(di + m * dj) * bs + 3 * k + a) * bs + 3 * k2 + c])
+                                        return false;
+                }
+    std::vector<cd> ex(m), ey(n);   // e^{2 pi i q / m}, e^{2 pi i q / n}
+    const double tau = 6.283185307179586476925286766559;
+    for (int q = 0; q < m; q++) ex[q] = std::polar(1.0, tau * q / m);
+    for (int q = 0; q < n; q++) ey[q] = std::polar(1.0, tau * q / n);
+    std::vector<cd> G((size_t)cols * bs * bs), D((size_t)bs * 2 * bs);
+    for (int ky = 0; ky < n; ky++)
+        for (int kx = 0; kx < m; kx++) {
+            // [D(t) | I], then Gauss-Jordan with partial pivoting
+            std::fill(D.begin(), D.end(), cd(0.0));
+            for (int dj = 0; dj < n; dj++)
+                for (int di = 0; di < m; di++) {
+                    const double *Ad = &A[(size_t)(di + m * dj) * bs * bs];
+                    bool any = false;
+                    for (int e = 0; e < bs * bs && !any; e++) any = Ad[e] != 0.0;
+                    if (!any) continue;
+                    const cd w = ex[(kx * di) % m] * ey[(ky * dj) % n];
+                    for (int r = 0; r < bs; r++)
+                        for (int c = 0; c < bs; c++) D[(size_t)r * 2 * bs + c] += Ad[r * bs + c] * w;
+                }
+            for (int r = 0; r < bs; r++) D[(size_t)r * 2 * bs + bs + r] = 1.0;
+            for (int col = 0; col < bs; col++) {
+                int piv = col;
+                for (int r = col + 1; r < bs; r++)
+                    if (std::abs(D[(size_t)r * 2 * bs + col]) > std::abs(D[(size_t)piv * 2 * bs + col])) piv = r;
+                const double pv = std::abs(D[(size_t)piv * 2 * bs + col]);
+                if (!(pv > 0.0) || !std::isfinite(pv)) fail(STZ_MG_ERR_SINGULAR, "bottom-level matrix is singular");
+                if (piv != col)
+                    for (int c = 0; c < 2 * bs; c++) std::swap(D[(size_t)piv * 2 * bs + c], D[(size_t)col * 2 * bs + c]);
+                const cd ip = 1.0 / D[(size_t)col * 2 * bs + col];
+                for (int c = 0; c < 2 * bs; c++) D[(size_t)col * 2 * bs + c] *= ip;
+                for (int r = 0; r < bs; r++) {
+                    if (r == col) continue;
+                    const cd f = D[(size_t)r * 2 * bs + col];
+                    if (f == cd(0.0)) continue;
+                    for (int c = 0; c < 2 * bs; c++) D[(size_t)r * 2 * bs + c] -= f * D[(size_t)col * 2 * bs + c];
+                }
+            }
+            cd *Gt = &G[(size_t)(kx + m * ky) * bs * bs];
+            for (int r = 0; r < bs; r++)
+                for (int c = 0; c < bs; c++) Gt[r * bs + c] = D[(size_t)r * 2 * bs + bs + c];
+        }
+    // B(d), then every block of the inverse
+    std::vector<double> B((size_t)cols * bs * bs);
+    std::vector<cd> acc((size_t)bs * bs);
+    for (int dj = 0; dj < n; dj++)
+        for (int di = 0; di < m; di++) {
+            std::fill(acc.begin(), acc.end(), cd(0.0));
+            for (int ky = 0; ky < n; ky++)
+                for (int kx = 0; kx < m; kx++) {
+                    const cd w = std::conj(ex[(kx * di) % m] * ey[(ky * dj) % n]);
+                    const cd *Gt = &G[(size_t)(kx + m * ky) * bs * bs];
+                    for (int e = 0; e < bs * bs; e++) acc[e] += Gt[e] * w;
+                }
+            double *Bd = &B[(size_t)(di + m * dj) * bs * bs];
+            for (int e = 0; e < bs * bs; e++) Bd[e] = acc[e].real() / cols;
+        }
+    inv.assign((size_t)nr * nr, 0.0);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++)
+            for (int k = 0; k < o; k++)
+                for (int a = 0; a < 3; a++) {
+                    double *r = &inv[row(i, j, k, a) * nr];
+                    for (int dj = 0; dj < n; dj++)
+                        for (int di = 0; di < m; di++) {
+                            const double *Bd = &B[((size_t)(di + m * dj) * bs + 3 * k + a) * bs];
+                            for (int k2 = 0; k2 < o; k2++)
+                                for (int c = 0; c < 3; c++) r[row((i + di) % m, (j + dj) % n, k2, c)] = Bd[3 * k2 + c];
+                        }
+                }
+    return true;
+}
+
 void build_bottom(stz_mg_handle h) {
     const int lb = h->nlev - 1;
     const Geom &g = h->geo[lb];
@@ -457,22 +570,14 @@ void build_bottom(stz_mg_handle h) {
                                 for (int c = 0; c < 3; c++) M[(3 * p + a) * nr + 3 * q + c] += blk[3 * a + c];
                         }
             }
-    // Gauss-Jordan inverse with partial pivoting, FP64, on the device.
-    std::vector<double> aug((size_t)nr * 2 * nr, 0.0);
-    for (int r = 0; r < nr; r++) {
-        std::memcpy(&aug[(size_t)r * 2 * nr], &M[(size_t)r * nr], nr * sizeof(double));
-        aug[(size_t)r * 2 * nr + nr + r] = 1.0;
-    }
     // buffers are sized by the bottom level, which does not change between set-ups
-    if (!h->bot_aug || h->nbot_rows != nr) {
+    if (!h->ainv_t || h->nbot_rows != nr) {
         h->release(h->bot_aug);
         h->release(h->bot_col);
         h->release(h->bot_piv);
         h->release(h->ainv_t);
         h->release(h->nat_slot);
-        h->bot_aug = h->alloc<double>(aug.size());
-        h->bot_col = h->alloc<double>(nr);
-        h->bot_piv = h->alloc<int>(1);
+        h->bot_aug = nullptr;
         h->ainv_t = h->alloc<double>((size_t)nr * nr);
         h->nat_slot = h->alloc<int>(N);
         std::vector<int> ns(N);
@@ -480,7 +585,33 @@ void build_bottom(stz_mg_handle h) {
             for (int j = 0; j < g.n; j++)
                 for (int i = 0; i < g.m; i++) ns[i + (size_t)g.m * (j + (size_t)g.n * k)] = slot(g, i, j, k);
         CK(cudaMemcpyAsync(h->nat_slot, ns.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        sync(h);
         h->nbot_rows = nr;
+    }
+    // a plane-invariant bottom periodic in x and y: Fourier blocks on the host
+    // (STZ_MG_BOTTOM_FOURIER=0 turns that off)
+    const char *fe = std::getenv("STZ_MG_BOTTOM_FOURIER");
+    const bool fourier_ok = !(fe && std::atoi(fe) == 0) && h->op64[lb].kind == OP_PLANE;
+    {
+        std::vector<double> inv;
+        if (fourier_ok && fourier_bottom_inverse(g, M, nr, inv)) {
+            CK(cudaMemcpyAsync(h->ainv_t, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+            sync(h);
+            h->bottom_fourier = true;
+            return;
+        }
+    }
+    h->bottom_fourier = false;
+    // Gauss-Jordan inverse with partial pivoting, FP64, on the device.
+    std::vector<double> aug((size_t)nr * 2 * nr, 0.0);
+    for (int r = 0; r < nr; r++) {
+        std::memcpy(&aug[(size_t)r * 2 * nr], &M[(size_t)r * nr], nr * sizeof(double));
+        aug[(size_t)r * 2 * nr + nr + r] = 1.0;
+    }
+    if (!h->bot_aug) {
+        h->bot_aug = h->alloc<double>(aug.size());
+        h->bot_col = h->alloc<double>(nr);
+        h->bot_piv = h->alloc<int>(1);
     }
     CK(cudaMemcpyAsync(h->bot_aug, aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));

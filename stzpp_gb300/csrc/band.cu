@@ -122,6 +122,8 @@ struct BandArgs {
     Geom g;
     int c;          // plane parity of this launch
     int nbands;     // n / kBandRows
+    int nplanes;    // planes of parity c
+    int rev;        // planes taken from the top down
 };
 
 // Stage plane kk of a field (three components) into buffer plane p: boxes
@@ -154,18 +156,61 @@ __device__ __forceinline__ void stage_plane(const BandMaps &mp, const Geom &g, i
         }
 }
 
-// One colour (A, B) of plane k (buffer plane 1) on NR sub-rows J0 .. J0+NR-1
-// of this thread's sub-grid column I: new values from r (rr) and the staged
-// neighbours, in the arithmetic and order of const_row<T, true, false>, then
-// the centre solve.  Neighbour (dx, dy, dz) of a node of parity (A, B) lies in
-// colour ((A+dx)&1, (B+dy)&1) at column I + floor((A+dx)/2) (wrapped: base
-// index ib[0..2] for shifts -1, 0, +1) and staged row Jr + floor((B+dy)/2).
-template <typename T, int M2, bool JOUT, int A, int B, int NR>
-__device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (&ib)[3], const ConstOp<T> &op,
-                                            const T (&rr)[NR][3], T (&out)[NR][3]) {
+// One colour (A, B) of plane k (buffer plane 1) on up to NR sub-rows
+// T0 .. T0+NR-1 (those below NT) of this thread's sub-grid column I: new
+// values from r (rr) and the staged neighbours, in the arithmetic and order
+// of const_row<T, true, false>, then the centre solve.  Neighbour
+// (dx, dy, dz) of a node of parity (A, B) lies in colour ((A+dx)&1, (B+dy)&1)
+// at column I + floor((A+dx)/2) (wrapped: base index ib[0..2] for shifts -1,
+// 0, +1, which already include the rows T0) and staged row
+// Jr + floor((B+dy)/2), Jr = t + 1.
+// KIND: OP_CONST (the elasticity stencil shared by every interior node, op.cop)
+// or OP_PLANE (the row of coefficients of plane k, cf: 243 entries and the 9
+// of the inverse centre block, in shared memory; SPARSE: the structural
+// zeros of the coarse elasticity operators), with the arithmetic of
+// const_row<T, true, false> or plane_row_coef<T, SPARSE, false>.
+template <typename T, int M2, bool JOUT, int KIND, bool SPARSE, int A, int B, int NR>
+__device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (&ib)[3], const LevelOp<T> &op,
+                                            const T *cf, int nvalid, const T (&rr)[NR][3], T (&out)[NR][3]) {
+    constexpr bool CONST = KIND == OP_CONST;
+    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    if constexpr (!CONST) {
+        // a full coarse row: one block at a time (its three neighbour values,
+        // then its products), as plane_row_coef orders the products; all 78
+        // values at once would not fit in registers (nor would several rows)
+#pragma unroll 1
+        for (int u = 0; u < NR; u++) {
+            if (u >= nvalid) break;   // warp-uniform
+            const int Jr = u + 1;
+            T acc[3] = {rr[u][0], rr[u][1], rr[u][2]};
+            sfor<0, 27>([&](auto bi) {
+                constexpr int b = decltype(bi)::value;
+                if constexpr (b != 13) {
+                    constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+                    constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+                    constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+                    asm volatile("" ::: "memory");
+                    const int base = ib[sI + 1] + (Jr + sJ) * rowstep;
+                    T v[3];
+                    v[0] = s[base + woff<M2, JOUT>(1 + dz, 0, 0, ap + 2 * bp, 0)];
+                    v[1] = s[base + woff<M2, JOUT>(1 + dz, 1, 0, ap + 2 * bp, 0)];
+                    v[2] = s[base + woff<M2, JOUT>(1 + dz, 2, 0, ap + 2 * bp, 0)];
 #pragma unroll
-    for (int t = 0; t < NR; t++) {
-        const int Jr = t + 1;
+                    for (int e = 0; e < 9; e++)
+                        if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[9 * b + e] * v[e % 3];
+                }
+            });
+            const T *inv = cf + 243;
+            out[u][0] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+            out[u][1] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+            out[u][2] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int u = 0; u < NR; u++) {
+        if (u >= nvalid) break;   // warp-uniform
+        const int Jr = u + 1;
         T v[27][3];
         sfor<0, 27>([&](auto bi) {
             constexpr int b = decltype(bi)::value;
@@ -182,18 +227,18 @@ __device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (
                 });
             }
         });
-        T acc[3] = {rr[t][0], rr[t][1], rr[t][2]};
+        T acc[3] = {rr[u][0], rr[u][1], rr[u][2]};
 #pragma unroll
         for (int b = 0; b < 27; b++) {
             if (b == 13 || nnz_axes(b) == 3) continue;
 #pragma unroll
             for (int e = 0; e < 9; e++)
-                if (elastic_entry(b, e)) acc[e / 3] -= op.a[b][e] * v[b][e % 3];
+                if (elastic_entry(b, e)) acc[e / 3] -= op.cop.a[b][e] * v[b][e % 3];
         }
-        const T *inv = op.inv_int;
-        out[t][0] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
-        out[t][1] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
-        out[t][2] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
+        const T *inv = op.cop.inv_int;
+        out[u][0] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
+        out[u][1] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
+        out[u][2] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
     }
 }
 
@@ -202,82 +247,111 @@ __device__ __forceinline__ size_t band_slot(const Geom &g, int ab, int c, int K,
     return (size_t)(ab + 4 * c) * g.S + ((size_t)K * g.N2 + J) * g.M2 + I;
 }
 
-template <typename T, int M2, bool JOUT>
-__global__ void __launch_bounds__(M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
-    gs_band_kernel(const BandArgs args, const __grid_constant__ ConstOp<T> op, const __grid_constant__ BandMaps in,
+// Rows of a colour per thread: colours 0 and 1 run on kOwnSub + 1 sub-rows,
+// 2 and 3 on kOwnSub; NH threads share a column, thread h taking rows
+// h * per .. (the rest of the column when fewer).
+template <int NRT, int NH>
+constexpr int kPer = (NRT + NH - 1) / NH;
+
+template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+__global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
+    gs_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op, const __grid_constant__ BandMaps in,
                    const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
     extern __shared__ __align__(128) unsigned char band_smem[];
     __shared__ __align__(8) unsigned long long bar_store;
+    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
     const Geom &g = args.g;
-    const int I = threadIdx.x;
-    const int band = blockIdx.x % args.nbands, kidx = blockIdx.x / args.nbands;
+    const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
+    const int band = blockIdx.x % args.nbands, kraw = blockIdx.x / args.nbands;
+    const int kidx = args.rev ? args.nplanes - 1 - kraw : kraw;
     const int c = args.c, k = 2 * kidx + c, K = kidx;
     const int J0 = band * kOwnSub;
     const size_t np = (size_t)g.npad;
     const bool zin = g.zp || (k != 0 && k != g.o - 1);
+    // planes k-1, k+1 exist (a Dirichlet z ends at the plates)
+    const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
 
-    if (!zin) {   // a Dirichlet plate: x = fix^-1 r, no neighbours
-        const T *inv = op.inv_fix;
+    if (KIND == OP_CONST && !zin) {   // a Dirichlet plate: x = fix^-1 r, no neighbours
+        const T *inv = op.cop.inv_fix;
 #pragma unroll 1
-        for (int ab = 0; ab < 4; ab++)
-#pragma unroll 1
-            for (int t = 0; t < kOwnSub; t++) {
-                const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
-                const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
-                xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
-                xout[sl + np] = dot3(inv[3], a0, inv[4], a1, inv[5], a2);
-                xout[sl + 2 * np] = dot3(inv[6], a0, inv[7], a1, inv[8], a2);
-            }
+        for (int w = hh; w < 4 * kOwnSub; w += NH) {
+            const int ab = w / kOwnSub, t = w % kOwnSub;
+            const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
+            const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
+            xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
+            xout[sl + np] = dot3(inv[3], a0, inv[4], a1, inv[5], a2);
+            xout[sl + 2 * np] = dot3(inv[6], a0, inv[7], a1, inv[8], a2);
+        }
         return;
     }
 
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
     const unsigned bar = (unsigned)__cvta_generic_to_shared(&bar_store);
-    if (I == 0) {
+    if (tid == 0) {
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     // TMA boxes land at 128-byte aligned shared addresses only
     const bool aligned = (sbase & 127u) == 0;
-    if (I == 0 && aligned) {
-        // every box of the three planes, announced before any is issued
-        mbar_expect_tx(bar, (unsigned)(kBandWords<M2> * sizeof(T)));
+    if (tid == 0 && aligned) {
+        // every box of the planes that exist, announced before any is issued
+        const unsigned plane_bytes = (unsigned)(kBandWords<M2> / 3 * sizeof(T));
+        mbar_expect_tx(bar, plane_bytes * (1u + has_lo + has_hi));
         // the z-neighbour planes: old values (x_in) under the even launch,
         // new ones (x_out) under the odd launch; plane k itself from x_in
         const BandMaps &zm = c == 0 ? in : out_maps;
         const int klo = k == 0 ? g.o - 1 : k - 1, khi = k == g.o - 1 ? 0 : k + 1;
-        stage_plane<T, M2, JOUT>(zm, g, klo, J0, 0, sbase, bar);
+        if (has_lo) stage_plane<T, M2, JOUT>(zm, g, klo, J0, 0, sbase, bar);
         stage_plane<T, M2, JOUT>(in, g, k, J0, 1, sbase, bar);
-        stage_plane<T, M2, JOUT>(zm, g, khi, J0, 2, sbase, bar);
+        if (has_hi) stage_plane<T, M2, JOUT>(zm, g, khi, J0, 2, sbase, bar);
     }
     if (!aligned) {
-        if (I == 0) atomicExch(&g_band_err, 2);
+        if (tid == 0) atomicExch(&g_band_err, 2);
         return;
     }
+    if (KIND == OP_PLANE) {
+        // plane k's row of coefficients; a missing neighbour plane reads as
+        // zeros (the colour kernels' neighbour outside the grid)
+        for (int e = tid; e < 252; e += NH * M2)
+            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+        T *sz = reinterpret_cast<T *>(band_smem);
+        constexpr int PW = kBandWords<M2> / 3;
+        if (!has_lo)
+            for (int w = tid; w < PW; w += NH * M2) sz[w] = T(0);
+        if (!has_hi)
+            for (int w = tid; w < PW; w += NH * M2) sz[2 * PW + w] = T(0);
+    }
+    // this thread's rows of each colour
+    constexpr int P0 = kPer<kOwnSub + 1, NH>, P1 = kPer<kOwnSub, NH>;
+    const int t0a = hh * P0, t0b = hh * P1;
+    const int na = min(P0, kOwnSub + 1 - t0a), nb = min(P1, kOwnSub - t0b);
     // r of every node this thread updates, while the boxes are in flight
-    T r0[kOwnSub + 1][3], r1[kOwnSub + 1][3], r2[kOwnSub][3], r3[kOwnSub][3];
+    T r0[P0][3], r1[P0][3], r2[P1][3], r3[P1][3];
 #pragma unroll
-    for (int t = 0; t <= kOwnSub; t++) {
-        const int J = J0 + t == g.N2 ? 0 : J0 + t;
+    for (int u = 0; u < P0; u++) {
+        if (u >= na) break;
+        const int J = J0 + t0a + u == g.N2 ? 0 : J0 + t0a + u;
         const size_t s0 = band_slot(g, 0, c, K, J, I), s1 = band_slot(g, 1, c, K, J, I);
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
-            r0[t][cc] = r[s0 + cc * np];
-            r1[t][cc] = r[s1 + cc * np];
+            r0[u][cc] = r[s0 + cc * np];
+            r1[u][cc] = r[s1 + cc * np];
         }
-        if (t < kOwnSub) {
-            const size_t s2 = band_slot(g, 2, c, K, J, I), s3 = band_slot(g, 3, c, K, J, I);
+    }
 #pragma unroll
-            for (int cc = 0; cc < 3; cc++) {
-                r2[t][cc] = r[s2 + cc * np];
-                r3[t][cc] = r[s3 + cc * np];
-            }
+    for (int u = 0; u < P1; u++) {
+        if (u >= nb) break;
+        const size_t s2 = band_slot(g, 2, c, K, J0 + t0b + u, I), s3 = band_slot(g, 3, c, K, J0 + t0b + u, I);
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            r2[u][cc] = r[s2 + cc * np];
+            r3[u][cc] = r[s3 + cc * np];
         }
     }
     const bool ok = mbar_wait(bar, 0, 200000000ull);   // 0.2 s: copies that never arrive
     if (!__syncthreads_and(ok)) {
-        if (I == 0) {
+        if (tid == 0) {
             atomicExch(&g_band_err, 1);
             mbar_wait(bar, 0, 200000000ull);   // let copies still in flight land before the CTA leaves
         }
@@ -286,50 +360,54 @@ __global__ void __launch_bounds__(M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
     }
 
     T *s = reinterpret_cast<T *>(band_smem);
-    const int ib[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
     constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    const int ibx[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
+    const int iba[3] = {ibx[0] + t0a * rowstep, ibx[1] + t0a * rowstep, ibx[2] + t0a * rowstep};
+    const int ibb[3] = {ibx[0] + t0b * rowstep, ibx[1] + t0b * rowstep, ibx[2] + t0b * rowstep};
     // store a colour's new values: shared memory for the later colours, x_out
     // for the rows this band owns
-    auto emit = [&](auto A_, auto B_, auto NR_, const auto &o, bool to_smem) {
+    auto emit = [&](auto A_, auto B_, auto NR_, int t0, int nv, const auto &o, bool to_smem) {
         constexpr int A = decltype(A_)::value, B = decltype(B_)::value, NR = decltype(NR_)::value;
 #pragma unroll
-        for (int t = 0; t < NR; t++) {
+        for (int u = 0; u < NR; u++) {
+            if (u >= nv) break;
+            const int t = t0 + u;
             if (to_smem)
 #pragma unroll
-                for (int cc = 0; cc < 3; cc++) s[I + woff<M2, JOUT>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[t][cc];
+                for (int cc = 0; cc < 3; cc++) s[I + woff<M2, JOUT>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[u][cc];
             if (t < kOwnSub) {
                 const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
 #pragma unroll
-                for (int cc = 0; cc < 3; cc++) xout[sl + cc * np] = o[t][cc];
+                for (int cc = 0; cc < 3; cc++) xout[sl + cc * np] = o[u][cc];
             }
         }
     };
     using I0 = std::integral_constant<int, 0>;
     using I1 = std::integral_constant<int, 1>;
-    using NRb0 = std::integral_constant<int, kOwnSub + 1>;
-    using NRb1 = std::integral_constant<int, kOwnSub>;
+    using NR0 = std::integral_constant<int, P0>;
+    using NR1 = std::integral_constant<int, P1>;
     {
-        T o[kOwnSub + 1][3];
-        band_colour<T, M2, JOUT, 0, 0, kOwnSub + 1>(s, ib, op, r0, o);
-        emit(I0{}, I0{}, NRb0{}, o, true);
+        T o[P0][3];
+        band_colour<T, M2, JOUT, KIND, SPARSE, 0, 0, P0>(s, iba, op, cfs, na, r0, o);
+        emit(I0{}, I0{}, NR0{}, t0a, na, o, true);
     }
     __syncthreads();
     {
-        T o[kOwnSub + 1][3];
-        band_colour<T, M2, JOUT, 1, 0, kOwnSub + 1>(s, ib, op, r1, o);
-        emit(I1{}, I0{}, NRb0{}, o, true);
+        T o[P0][3];
+        band_colour<T, M2, JOUT, KIND, SPARSE, 1, 0, P0>(s, iba, op, cfs, na, r1, o);
+        emit(I1{}, I0{}, NR0{}, t0a, na, o, true);
     }
     __syncthreads();
     {
-        T o[kOwnSub][3];
-        band_colour<T, M2, JOUT, 0, 1, kOwnSub>(s, ib, op, r2, o);
-        emit(I0{}, I1{}, NRb1{}, o, true);
+        T o[P1][3];
+        band_colour<T, M2, JOUT, KIND, SPARSE, 0, 1, P1>(s, ibb, op, cfs, nb, r2, o);
+        emit(I0{}, I1{}, NR1{}, t0b, nb, o, true);
     }
     __syncthreads();
     {
-        T o[kOwnSub][3];
-        band_colour<T, M2, JOUT, 1, 1, kOwnSub>(s, ib, op, r3, o);
-        emit(I1{}, I1{}, NRb1{}, o, false);
+        T o[P1][3];
+        band_colour<T, M2, JOUT, KIND, SPARSE, 1, 1, P1>(s, ibb, op, cfs, nb, r3, o);
+        emit(I1{}, I1{}, NR1{}, t0b, nb, o, false);
     }
 }
 
@@ -420,11 +498,17 @@ bool first_band_use(unsigned long long &devices) {
     return true;
 }
 
-template <typename T, int M2, bool JOUT>
+// Threads per column of the band kernel: two in FP32 (twice the warps for
+// the same shared memory), one in FP64 (one CTA per SM, registers)
+template <typename T>
+constexpr int kBandNH = sizeof(T) == 4 ? 2 : 1;
+
+template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
 bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     BandMaps min_, mout;
     if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
-    auto kern = gs_band_kernel<T, M2, JOUT>;
+    constexpr int NH = kBandNH<T>;
+    auto kern = gs_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);
     static unsigned long long attr_devices = 0;
     if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -435,19 +519,31 @@ bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin
         const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
         if (planes <= 0) continue;
         a.c = c;
-        kern<<<a.nbands * planes, M2, smem, st>>>(a, op.cop, min_, mout, r, xout);
+        a.nplanes = planes;
+        // the odd launch walks down from where the even one ended, so its
+        // first planes (and the even planes they read) are still in L2; the
+        // next sweep's even launch starts at the bottom, where this one ends
+        a.rev = c;
+        kern<<<a.nbands * planes, NH * M2, smem, st>>>(a, op, min_, mout, r, xout);
     }
     return true;
 }
 
-template <typename T, bool JOUT>
+template <typename T, bool JOUT, int KIND, bool SPARSE>
 bool launch_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     switch (g.M2) {
-        case 32: return launch_band_k<T, 32, JOUT>(op, g, r, xin, xout, st);
-        case 64: return launch_band_k<T, 64, JOUT>(op, g, r, xin, xout, st);
-        case 128: return launch_band_k<T, 128, JOUT>(op, g, r, xin, xout, st);
+        case 32: return launch_band_k<T, 32, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 64: return launch_band_k<T, 64, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 128: return launch_band_k<T, 128, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
         default: return false;
     }
+}
+
+template <typename T, bool JOUT>
+bool launch_band_op(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+    if (op.kind == OP_CONST) return launch_band_m<T, JOUT, OP_CONST, false>(op, g, r, xin, xout, st);
+    if (op.pop.sparse) return launch_band_m<T, JOUT, OP_PLANE, true>(op, g, r, xin, xout, st);
+    return launch_band_m<T, JOUT, OP_PLANE, false>(op, g, r, xin, xout, st);
 }
 
 }  // namespace
@@ -463,7 +559,7 @@ bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
     if (const char *e = std::getenv("STZ_MG_BAND")) mode = std::atoi(e) != 0;
     if (mode == 0) return false;
     if (mode < 0 && sizeof(T) != 4) return false;
-    if (op.kind != OP_CONST || !op.cop.elastic) return false;
+    if (!((op.kind == OP_CONST && op.cop.elastic) || op.kind == OP_PLANE)) return false;
     if (!g.xp || !g.yp || (g.m & 1) || g.n % kBandRows != 0 || g.n < 2 * kBandRows) return false;
     if (g.M2 != 32 && g.M2 != 64 && g.M2 != 128) return false;
     if (g.zp && (g.o & 1)) return false;
@@ -475,8 +571,8 @@ bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
 template <typename T>
 bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     const int layout = band_layout<T>(g, xin);
-    if (layout == 1) return launch_band_m<T, true>(op, g, r, xin, xout, st);
-    if (layout == 0) return launch_band_m<T, false>(op, g, r, xin, xout, st);
+    if (layout == 1) return launch_band_op<T, true>(op, g, r, xin, xout, st);
+    if (layout == 0) return launch_band_op<T, false>(op, g, r, xin, xout, st);
     return false;
 }
 

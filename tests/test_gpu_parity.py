@@ -322,33 +322,39 @@ def test_tiled_sweep_mixed_solve_bitwise(dims, per, kind, monkeypatch):
     assert np.array_equal(out["0"][2], out["1"][2])
 
 
-BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), 2), ((64, 64, 16), (True, True, True), 2),
-                    ((128, 64, 9), (True, True, False), 3), ((128, 128, 8), (True, True, True), 2),
-                    ((256, 256, 9), (True, True, False), 2), ((64, 16, 5), (True, True, False), 4)]
+BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64, 16), (True, True, True), "const", 0, 2),
+                    ((128, 64, 9), (True, True, False), "const", 0, 3), ((128, 128, 8), (True, True, True), "const", 0, 2),
+                    ((256, 256, 9), (True, True, False), "const", 0, 2), ((64, 16, 5), (True, True, False), "const", 0, 4),
+                    ((128, 128, 17), (True, True, False), "const", 1, 2), ((128, 128, 16), (True, True, True), "const", 1, 3),
+                    ((128, 64, 17), (True, True, False), "trans", 1, 2), ((256, 128, 10), (True, True, False), "trans", 1, 2)]
 
 
-@pytest.mark.parametrize("dims,per,sweeps", BAND_LEVEL_CASES)
-def test_band_sweep_is_the_colour_sweep(dims, per, sweeps, monkeypatch):
-    """The band sweep of the fine level (full-width bands of 8 rows, planes
-    staged by TMA boxes, split at the periodic wrap in y) gives bit for bit the
-    result of the eight colour launches: FP64 level sweeps of the elasticity
-    stencil, Dirichlet and periodic z, 32, 64 and 128 sub-grid columns, two
-    bands (both at the wrap) and many, even and odd sweep counts."""
+@pytest.mark.parametrize("dims,per,kind,level,sweeps", BAND_LEVEL_CASES)
+def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, monkeypatch):
+    """The band sweep (full-width bands of 8 rows, planes staged by TMA boxes,
+    split at the periodic wrap in y) gives bit for bit the result of the eight
+    colour launches: FP64 level sweeps of the elasticity stencil on the fine
+    level and of the plane-invariant coarse operators (sparse elastic and
+    full from a non-symmetric stencil) on level 1, Dirichlet and periodic z,
+    32, 64 and 128 sub-grid columns, two bands (both at the wrap) and many,
+    even and odd sweep counts."""
     import stzpp_gb300 as sg
     m, n, o = dims
-    st, fix = sg.elastic_stencil(1.0, 2.0, *P.grid_spacing(m, n, o, per))
+    h = P.grid_spacing(m, n, o, per)
+    st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(2, h[0])
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
         monkeypatch.setenv("STZ_MG_TILE", "0")
-        with sg.Multigrid(dims, per, precision="fp64", bottom="gs", max_coarse=10 ** 6) as mg:
+        with sg.Multigrid(dims, per, precision="fp64", bottom="gs", max_coarse=10 ** 6 if level == 0 else 5000) as mg:
             mg.setup_matrices(stencil=st, fix=fix)
-            N = mg.level_npts(0)
+            assert (mg.sweep_kind(level)[0] == "band") == (band == "1")
+            N = mg.level_npts(level)
             rng = np.random.default_rng(11)
-            mg.level_set_field(0, "x", rng.standard_normal((N, 3)))
-            mg.level_set_field(0, "r", rng.standard_normal((N, 3)))
-            mg.gauss_seidel(0, sweeps)
-            out[band] = mg.level_get_field(0, "x")
+            mg.level_set_field(level, "x", rng.standard_normal((N, 3)))
+            mg.level_set_field(level, "r", rng.standard_normal((N, 3)))
+            mg.gauss_seidel(level, sweeps)
+            out[band] = mg.level_get_field(level, "x")
     assert np.array_equal(out["0"], out["1"])
 
 
@@ -400,3 +406,30 @@ def test_cluster_tail_is_the_level_graph(precision, monkeypatch):
             out[tail] = (cyc, rel, mg.get_x())
     assert out["0"][:2] == out["1"][:2]
     assert np.array_equal(out["0"][2], out["1"][2])
+
+
+@pytest.mark.parametrize("dims,kind,precision", [((64, 64, 65), "const", "fp64"), ((64, 64, 65), "trans", "fp64"),
+                                                 ((32, 32, 33), "const", "mixed"), ((96, 64, 16), "trans", "fp64")])
+def test_fourier_bottom_inverse_is_the_dense_inverse(dims, kind, precision, monkeypatch):
+    """The bottom inverse of a plane-invariant operator periodic in x and y
+    from its Fourier blocks (m n complex systems of order 3o) against the
+    dense Gauss-Jordan inverse: the same cycle count, solutions to 1e-12,
+    and the bottom level's operator applied to the inverse's output gives
+    back its input (through whole solves: the reference's own hierarchy)."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    per = (True, True, False)
+    h = P.grid_spacing(m, n, o, per, h=1.0 / m)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(1, h[0])
+    out = {}
+    for fourier in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_BOTTOM_FOURIER", fourier)
+        with sg.Multigrid(dims, per, precision=precision, sweep_growth=False, v_down=2, v_up=3) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-12 if precision == "fp64" else 1e-10, 60)
+            out[fourier] = (cyc, mg.get_x())
+    assert out["0"][0] == out["1"][0]
+    x0, x1 = out["0"][1], out["1"][1]
+    assert np.linalg.norm(x1 - x0) <= 1e-11 * np.linalg.norm(x0)
