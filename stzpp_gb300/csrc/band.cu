@@ -253,80 +253,84 @@ __device__ __forceinline__ size_t band_slot(const Geom &g, int ab, int c, int K,
 template <int NRT, int NH>
 constexpr int kPer = (NRT + NH - 1) / NH;
 
+// One work item of a launch: band `band` of plane k (parity args.c).
+struct BandItem {
+    int band, k, K, J0;
+    bool zin, has_lo, has_hi;
+};
+
+__device__ __forceinline__ BandItem band_item(const BandArgs &args, int item) {
+    const Geom &g = args.g;
+    BandItem it;
+    it.band = item % args.nbands;
+    const int kraw = item / args.nbands;
+    it.K = args.rev ? args.nplanes - 1 - kraw : kraw;
+    it.k = 2 * it.K + args.c;
+    it.J0 = it.band * kOwnSub;
+    it.zin = g.zp || (it.k != 0 && it.k != g.o - 1);
+    // planes k-1, k+1 exist (a Dirichlet z ends at the plates)
+    it.has_lo = g.zp || it.k > 0;
+    it.has_hi = g.zp || it.k < g.o - 1;
+    return it;
+}
+
+// Whether an item stages planes (a plate of the shared stencil does not).
+template <int KIND>
+__device__ __forceinline__ bool band_stages(const BandItem &it) {
+    return KIND == OP_PLANE || it.zin;
+}
+
+// Thread 0: the boxes of an item's planes into the buffer at sbuf,
+// completing on bar (every byte announced before any box is issued).
+template <typename T, int M2, bool JOUT>
+__device__ __forceinline__ void band_issue(const BandArgs &args, const BandMaps &in, const BandMaps &out_maps,
+                                           const BandItem &it, unsigned sbuf, unsigned bar) {
+    const Geom &g = args.g;
+    const unsigned plane_bytes = (unsigned)(kBandWords<M2> / 3 * sizeof(T));
+    mbar_expect_tx(bar, plane_bytes * (1u + it.has_lo + it.has_hi));
+    // the z-neighbour planes: old values (x_in) under the even launch, new
+    // ones (x_out) under the odd launch; plane k itself from x_in
+    const BandMaps &zm = args.c == 0 ? in : out_maps;
+    const int klo = it.k == 0 ? g.o - 1 : it.k - 1, khi = it.k == g.o - 1 ? 0 : it.k + 1;
+    if (it.has_lo) stage_plane<T, M2, JOUT>(zm, g, klo, it.J0, 0, sbuf, bar);
+    stage_plane<T, M2, JOUT>(in, g, it.k, it.J0, 1, sbuf, bar);
+    if (it.has_hi) stage_plane<T, M2, JOUT>(zm, g, khi, it.J0, 2, sbuf, bar);
+}
+
+// A Dirichlet plate of the shared stencil: x = fix^-1 r, no neighbours.
+template <typename T, int M2, int NH>
+__device__ __forceinline__ void band_plate(const Geom &g, const ConstOp<T> &op, const BandItem &it, int c,
+                                           const T *__restrict__ r, T *__restrict__ xout) {
+    const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
+    const size_t np = (size_t)g.npad;
+    const T *inv = op.inv_fix;
+#pragma unroll 1
+    for (int w = hh; w < 4 * kOwnSub; w += NH) {
+        const int ab = w / kOwnSub, t = w % kOwnSub;
+        const size_t sl = band_slot(g, ab, c, it.K, it.J0 + t, I);
+        const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
+        xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
+        xout[sl + np] = dot3(inv[3], a0, inv[4], a1, inv[5], a2);
+        xout[sl + 2 * np] = dot3(inv[6], a0, inv[7], a1, inv[8], a2);
+    }
+}
+
+// All threads: one staged item -- r of this thread's nodes (loaded while the
+// boxes are in flight), the wait for the boxes (phase `phase` of bar, at
+// most 0.2 s), then the plane's four colours.  False if the boxes did not
+// arrive (recorded; every thread returns false).
 template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
-__global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
-    gs_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op, const __grid_constant__ BandMaps in,
-                   const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
-    extern __shared__ __align__(128) unsigned char band_smem[];
-    __shared__ __align__(8) unsigned long long bar_store;
-    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+__device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp<T> &op, const BandItem &it, T *s,
+                                             T *cfs, unsigned bar, unsigned phase, const T *__restrict__ r,
+                                             T *__restrict__ xout) {
     const Geom &g = args.g;
     const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
-    const int band = blockIdx.x % args.nbands, kraw = blockIdx.x / args.nbands;
-    const int kidx = args.rev ? args.nplanes - 1 - kraw : kraw;
-    const int c = args.c, k = 2 * kidx + c, K = kidx;
-    const int J0 = band * kOwnSub;
+    const int c = args.c, K = it.K, J0 = it.J0, k = it.k;
     const size_t np = (size_t)g.npad;
-    const bool zin = g.zp || (k != 0 && k != g.o - 1);
-    // planes k-1, k+1 exist (a Dirichlet z ends at the plates)
-    const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
-
-    if (KIND == OP_CONST && !zin) {   // a Dirichlet plate: x = fix^-1 r, no neighbours
-        const T *inv = op.cop.inv_fix;
-#pragma unroll 1
-        for (int w = hh; w < 4 * kOwnSub; w += NH) {
-            const int ab = w / kOwnSub, t = w % kOwnSub;
-            const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
-            const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
-            xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
-            xout[sl + np] = dot3(inv[3], a0, inv[4], a1, inv[5], a2);
-            xout[sl + 2 * np] = dot3(inv[6], a0, inv[7], a1, inv[8], a2);
-        }
-        return;
-    }
-
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
-    const unsigned bar = (unsigned)__cvta_generic_to_shared(&bar_store);
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    // TMA boxes land at 128-byte aligned shared addresses only
-    const bool aligned = (sbase & 127u) == 0;
-    if (tid == 0 && aligned) {
-        // every box of the planes that exist, announced before any is issued
-        const unsigned plane_bytes = (unsigned)(kBandWords<M2> / 3 * sizeof(T));
-        mbar_expect_tx(bar, plane_bytes * (1u + has_lo + has_hi));
-        // the z-neighbour planes: old values (x_in) under the even launch,
-        // new ones (x_out) under the odd launch; plane k itself from x_in
-        const BandMaps &zm = c == 0 ? in : out_maps;
-        const int klo = k == 0 ? g.o - 1 : k - 1, khi = k == g.o - 1 ? 0 : k + 1;
-        if (has_lo) stage_plane<T, M2, JOUT>(zm, g, klo, J0, 0, sbase, bar);
-        stage_plane<T, M2, JOUT>(in, g, k, J0, 1, sbase, bar);
-        if (has_hi) stage_plane<T, M2, JOUT>(zm, g, khi, J0, 2, sbase, bar);
-    }
-    if (!aligned) {
-        if (tid == 0) atomicExch(&g_band_err, 2);
-        return;
-    }
-    if (KIND == OP_PLANE) {
-        // plane k's row of coefficients; a missing neighbour plane reads as
-        // zeros (the colour kernels' neighbour outside the grid)
-        for (int e = tid; e < 252; e += NH * M2)
-            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
-        T *sz = reinterpret_cast<T *>(band_smem);
-        constexpr int PW = kBandWords<M2> / 3;
-        if (!has_lo)
-            for (int w = tid; w < PW; w += NH * M2) sz[w] = T(0);
-        if (!has_hi)
-            for (int w = tid; w < PW; w += NH * M2) sz[2 * PW + w] = T(0);
-    }
     // this thread's rows of each colour
     constexpr int P0 = kPer<kOwnSub + 1, NH>, P1 = kPer<kOwnSub, NH>;
     const int t0a = hh * P0, t0b = hh * P1;
     const int na = min(P0, kOwnSub + 1 - t0a), nb = min(P1, kOwnSub - t0b);
-    // r of every node this thread updates, while the boxes are in flight
     T r0[P0][3], r1[P0][3], r2[P1][3], r3[P1][3];
 #pragma unroll
     for (int u = 0; u < P0; u++) {
@@ -349,17 +353,28 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
             r3[u][cc] = r[s3 + cc * np];
         }
     }
-    const bool ok = mbar_wait(bar, 0, 200000000ull);   // 0.2 s: copies that never arrive
+    if (KIND == OP_PLANE)   // plane k's row of coefficients
+        for (int e = tid; e < 252; e += NH * M2)
+            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+    const bool ok = mbar_wait(bar, phase, 200000000ull);   // 0.2 s: copies that never arrive
     if (!__syncthreads_and(ok)) {
         if (tid == 0) {
             atomicExch(&g_band_err, 1);
-            mbar_wait(bar, 0, 200000000ull);   // let copies still in flight land before the CTA leaves
+            mbar_wait(bar, phase, 200000000ull);   // let copies still in flight land before the CTA leaves
         }
         __syncthreads();
-        return;
+        return false;
     }
-
-    T *s = reinterpret_cast<T *>(band_smem);
+    if (KIND == OP_PLANE && !(it.has_lo && it.has_hi)) {
+        // a missing neighbour plane reads as zeros (the colour kernels'
+        // neighbour outside the grid)
+        constexpr int PW = kBandWords<M2> / 3;
+        if (!it.has_lo)
+            for (int w = tid; w < PW; w += NH * M2) s[w] = T(0);
+        if (!it.has_hi)
+            for (int w = tid; w < PW; w += NH * M2) s[2 * PW + w] = T(0);
+        __syncthreads();
+    }
     constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
     const int ibx[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
     const int iba[3] = {ibx[0] + t0a * rowstep, ibx[1] + t0a * rowstep, ibx[2] + t0a * rowstep};
@@ -408,6 +423,102 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
         T o[P1][3];
         band_colour<T, M2, JOUT, KIND, SPARSE, 1, 1, P1>(s, ibb, op, cfs, nb, r3, o);
         emit(I1{}, I1{}, NR1{}, t0b, nb, o, false);
+    }
+    return true;
+}
+
+// One CTA per work item.
+template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+__global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
+    gs_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op, const __grid_constant__ BandMaps in,
+                   const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
+    extern __shared__ __align__(128) unsigned char band_smem[];
+    __shared__ __align__(8) unsigned long long bar_store;
+    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+    const int tid = threadIdx.x;
+    const BandItem it = band_item(args, blockIdx.x);
+    if (!band_stages<KIND>(it)) {
+        band_plate<T, M2, NH>(args.g, op.cop, it, args.c, r, xout);
+        return;
+    }
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&bar_store);
+    if ((sbase & 127u) != 0) {   // TMA boxes land at 128-byte aligned shared addresses only
+        if (tid == 0) atomicExch(&g_band_err, 2);
+        return;
+    }
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) band_issue<T, M2, JOUT>(args, in, out_maps, it, sbase, bar);
+    band_compute<T, M2, JOUT, NH, KIND, SPARSE>(args, op, it, reinterpret_cast<T *>(band_smem), cfs, bar, 0, r, xout);
+}
+
+// Persistent form: one CTA per SM walks the items blockIdx.x, + gridDim.x,
+// ..., with two staging buffers: the boxes of the item after next are issued
+// as soon as an item's compute has released its buffer, so the copy engine
+// streams while the SM computes.  Buffer b's mbarrier completes once per
+// staged item it receives, so its phase parity is its count of staged items.
+template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+__global__ void __launch_bounds__(NH * M2, 1)
+    gs_band_persist_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op,
+                           const __grid_constant__ BandMaps in, const __grid_constant__ BandMaps out_maps,
+                           const T *__restrict__ r, T *__restrict__ xout) {
+    extern __shared__ __align__(128) unsigned char band_smem[];
+    __shared__ __align__(8) unsigned long long bar_store[2];
+    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+    const int tid = threadIdx.x;
+    const int nitems = args.nbands * args.nplanes, G = gridDim.x;
+    constexpr unsigned BUFB = kBandWords<M2> * sizeof(T);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
+    const unsigned bar0 = (unsigned)__cvta_generic_to_shared(&bar_store[0]);
+    if ((sbase & 127u) != 0) {
+        if (tid == 0) atomicExch(&g_band_err, 2);
+        return;
+    }
+    if (tid == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar0 + 8, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // the i-th item of this CTA uses buffer i & 1; items staged into each buffer so far
+    unsigned staged0 = 0, staged1 = 0;
+    if (tid == 0)
+        for (int i = 0; i < 2; i++) {
+            const int item = blockIdx.x + i * G;
+            if (item >= nitems) break;
+            const BandItem it = band_item(args, item);
+            if (band_stages<KIND>(it)) band_issue<T, M2, JOUT>(args, in, out_maps, it, sbase + i * BUFB, bar0 + 8 * i);
+        }
+    int i = 0;
+    for (int item = blockIdx.x; item < nitems; item += G, i++) {
+        const int buf = i & 1;
+        const BandItem it = band_item(args, item);
+        if (!band_stages<KIND>(it)) {
+            band_plate<T, M2, NH>(args.g, op.cop, it, args.c, r, xout);
+        } else {
+            T *s = reinterpret_cast<T *>(band_smem + buf * BUFB);
+            if (!band_compute<T, M2, JOUT, NH, KIND, SPARSE>(args, op, it, s, cfs, bar0 + 8 * buf,
+                                                             (buf ? staged1 : staged0) & 1, r, xout)) {
+                // the other buffer may still be receiving the next item's boxes
+                const int nxt = item + G;
+                if (tid == 0 && nxt < nitems && band_stages<KIND>(band_item(args, nxt)))
+                    mbar_wait(bar0 + 8 * (buf ^ 1), (buf ? staged0 : staged1) & 1, 200000000ull);
+                __syncthreads();
+                return;
+            }
+            if (buf) staged1++;
+            else staged0++;
+        }
+        __syncthreads();   // buffer buf (and cfs) free again
+        const int next = item + 2 * G;
+        if (tid == 0 && next < nitems) {
+            const BandItem nt = band_item(args, next);
+            if (band_stages<KIND>(nt)) band_issue<T, M2, JOUT>(args, in, out_maps, nt, sbase + buf * BUFB, bar0 + 8 * buf);
+        }
     }
 }
 
@@ -503,10 +614,48 @@ bool first_band_use(unsigned long long &devices) {
 template <typename T>
 constexpr int kBandNH = sizeof(T) == 4 ? 2 : 1;
 
+// The persistent double-buffered form (STZ_MG_BAND_PERSIST=1) or one CTA per item.
+bool band_persist() {
+    const char *e = std::getenv("STZ_MG_BAND_PERSIST");
+    return e && std::atoi(e) != 0;
+}
+
+template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
+bool launch_band_persist(const LevelOp<T> &op, const Geom &g, const T *r, const BandMaps &min_,
+                         const BandMaps &mout, T *xout, cudaStream_t st) {
+    constexpr int NH = sizeof(T) == 4 ? 4 : 1;
+    auto kern = gs_band_persist_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
+    const int smem = 2 * kBandWords<M2> * (int)sizeof(T);
+    static unsigned long long attr_devices = 0;
+    static int per_sm = 0, sms = 0;
+    if (first_band_use(attr_devices)) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NH * M2, smem);
+    }
+    if (per_sm < 1 || sms < 1) return false;
+    BandArgs a;
+    a.g = g;
+    a.nbands = g.n / kBandRows;
+    for (int c = 0; c < 2; c++) {
+        const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
+        if (planes <= 0) continue;
+        a.c = c;
+        a.nplanes = planes;
+        a.rev = c;
+        const int grid = std::min(a.nbands * planes, per_sm * sms);
+        kern<<<grid, NH * M2, smem, st>>>(a, op, min_, mout, r, xout);
+    }
+    return true;
+}
+
 template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
 bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     BandMaps min_, mout;
     if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
+    if (band_persist()) return launch_band_persist<T, M2, JOUT, KIND, SPARSE>(op, g, r, min_, mout, xout, st);
     constexpr int NH = kBandNH<T>;
     auto kern = gs_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);

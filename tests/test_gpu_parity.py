@@ -329,19 +329,22 @@ BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64
                     ((128, 64, 17), (True, True, False), "trans", 1, 2), ((256, 128, 10), (True, True, False), "trans", 1, 2)]
 
 
+@pytest.mark.parametrize("persist", ["0", "1"])
 @pytest.mark.parametrize("dims,per,kind,level,sweeps", BAND_LEVEL_CASES)
-def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, monkeypatch):
+def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, persist, monkeypatch):
     """The band sweep (full-width bands of 8 rows, planes staged by TMA boxes,
     split at the periodic wrap in y) gives bit for bit the result of the eight
     colour launches: FP64 level sweeps of the elasticity stencil on the fine
     level and of the plane-invariant coarse operators (sparse elastic and
     full from a non-symmetric stencil) on level 1, Dirichlet and periodic z,
     32, 64 and 128 sub-grid columns, two bands (both at the wrap) and many,
-    even and odd sweep counts."""
+    even and odd sweep counts; with a CTA per band and plane, and with the
+    persistent form (a CTA per SM, two staging buffers, STZ_MG_BAND_PERSIST=1)."""
     import stzpp_gb300 as sg
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per)
     st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(2, h[0])
+    monkeypatch.setenv("STZ_MG_BAND_PERSIST", persist)
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
@@ -358,9 +361,10 @@ def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, monkeypa
     assert np.array_equal(out["0"], out["1"])
 
 
+@pytest.mark.parametrize("persist", ["0", "1"])
 @pytest.mark.parametrize("dims,per", [((128, 128, 33), (True, True, False)), ((256, 256, 17), (True, True, False)),
                                       ((128, 64, 24), (True, True, False))])
-def test_band_sweep_mixed_solve_bitwise(dims, per, monkeypatch):
+def test_band_sweep_mixed_solve_bitwise(dims, per, persist, monkeypatch):
     """The FP32 V-cycles of the mixed solve with the band sweep on the fine
     level (the default) and with the colour launches give the same cycle
     count and the same solution bit for bit (an even plane count puts the
@@ -369,6 +373,7 @@ def test_band_sweep_mixed_solve_bitwise(dims, per, monkeypatch):
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per, h=1.0 / m)
     b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    monkeypatch.setenv("STZ_MG_BAND_PERSIST", persist)
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
