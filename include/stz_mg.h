@@ -44,7 +44,7 @@ enum {
 enum { STZ_MG_FP64 = 0, STZ_MG_MIXED = 1 };          /* precision */
 enum { STZ_MG_BOTTOM_DIRECT = 0, STZ_MG_BOTTOM_GS = 1 };
 enum { STZ_MG_HOST = 0, STZ_MG_DEVICE = 1 };        /* where a pointer lives */
-enum { STZ_MG_FIELD_X = 0, STZ_MG_FIELD_R = 1 };
+enum { STZ_MG_FIELD_X = 0, STZ_MG_FIELD_R = 1, STZ_MG_FIELD_RES = 2 };   /* a level's x, r, residual work field */
 
 typedef struct stz_mg_handle_s *stz_mg_handle;
 
@@ -194,6 +194,22 @@ int stz_mg_level_restriction(stz_mg_handle h, int level);
 int stz_mg_level_interpolation(stz_mg_handle h, int level);
 /* region::residual (region.cc:1008) of every node, 3*npts doubles (may be NULL), and sum |r|^2 */
 int stz_mg_level_residual(stz_mg_handle h, int level, double *out, double *sumsq, int where);
+
+/* Pieces of a decomposed sweep and transfer, for callers that split the grid
+ * over several handles (stzpp_gb300/slabs.py: z-slabs exchanging ghost planes,
+ * the reference's MPI decomposition of region.cc:2759-2910).
+ * z-planes k0 .. k0+nk-1 of a level's field (STZ_MG_FIELD_X, _R or _RES) to or
+ * from 3*m*n*nk doubles in natural order (x fastest) -- the planes a
+ * neighbour sub-domain needs (region::communicate, region.cc:2759-2847). */
+int stz_mg_level_get_planes(stz_mg_handle h, int level, int which, int k0, int nk, double *v, int where);
+int stz_mg_level_set_planes(stz_mg_handle h, int level, int which, int k0, int nk, const double *v, int where);
+/* Colour passes q0 .. q1-1 of the 8-colour Gauss-Seidel sweep of a level (FP64);
+ * a sweep split where a sub-domain exchanges its ghost planes. */
+int stz_mg_level_gs_colours(stz_mg_handle h, int level, int q0, int q1);
+/* multigrid::restriction (multigrid.cc:436-449) from the level-1 residual
+ * field as it stands (STZ_MG_FIELD_RES, e.g. with ghost planes filled in by a
+ * neighbour) instead of recomputing it; coarse x = 0. */
+int stz_mg_level_restrict_residual(stz_mg_handle h, int level);
 
 /* Measurement hook (no counterpart in the reference): launches one kernel of
  * the solver `reps` times on the handle's stream between CUDA events and

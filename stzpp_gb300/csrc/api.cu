@@ -353,6 +353,32 @@ __global__ void sumsq_partial_kernel(const double *__restrict__ v, size_t n, dou
     }
 }
 
+// z-planes k0 .. k0+nk-1 of a colour-blocked FP64 vec3 field <-> natural
+// order (x fastest, 3 doubles per node, the planes' nodes only).
+__global__ void planes_cb_to_nat_kernel(Geom g, int k0, int nk, const double *__restrict__ cb,
+                                        double *__restrict__ nat) {
+    const long long n = (long long)g.m * g.n * nk;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.m), j = (int)((t / g.m) % g.n), k = k0 + (int)(t / ((long long)g.m * g.n));
+        const int s = slot(g, i, j, k);
+        nat[3 * t] = cb[s];
+        nat[3 * t + 1] = cb[s + g.npad];
+        nat[3 * t + 2] = cb[s + 2 * (size_t)g.npad];
+    }
+}
+
+__global__ void planes_nat_to_cb_kernel(Geom g, int k0, int nk, const double *__restrict__ nat,
+                                        double *__restrict__ cb) {
+    const long long n = (long long)g.m * g.n * nk;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.m), j = (int)((t / g.m) % g.n), k = k0 + (int)(t / ((long long)g.m * g.n));
+        const int s = slot(g, i, j, k);
+        cb[s] = nat[3 * t];
+        cb[s + g.npad] = nat[3 * t + 1];
+        cb[s + 2 * (size_t)g.npad] = nat[3 * t + 2];
+    }
+}
+
 // region::l2_error_all for vec3 (region.cc:3030-3057): sum over nodes of
 // mg3d_mod_sq(|r|^2) = |r|^4, from the colour-blocked FP64 residual (3 planes
 // of npad; the slots of no node hold zero).  One partial per block, fixed
@@ -1490,13 +1516,21 @@ int stz_mg_level_operator(stz_mg_handle h, int level, double *A, int *S) {
     });
 }
 
+// The FP64 field `which` of a level.
+double *level_field(stz_mg_handle h, int level, int which) {
+    if (which == STZ_MG_FIELD_X) return h->L64[level].x;
+    if (which == STZ_MG_FIELD_R) return h->L64[level].r;
+    if (which == STZ_MG_FIELD_RES) return h->L64[level].res;
+    fail(STZ_MG_ERR_ARG, "which must be STZ_MG_FIELD_X, _R or _RES");
+}
+
 int stz_mg_level_set_field(stz_mg_handle h, int level, int which, const double *v, int where) {
     if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
     return guarded(h, [&] {
         check_level(h, level);
         const Geom &g = h->geo[level];
+        double *dst = level_field(h, level, which);
         const double *src = to_device(h, v, 3 * npts(g), where);
-        double *dst = which == STZ_MG_FIELD_X ? h->L64[level].x : h->L64[level].r;
         launch_nat_to_cb<double>(g, src, dst, h->st);
         check_launch();
         if (level == 0 && which == STZ_MG_FIELD_R) h->bnorm = -1.0;
@@ -1510,11 +1544,75 @@ int stz_mg_level_get_field(stz_mg_handle h, int level, int which, double *v, int
         check_level(h, level);
         const Geom &g = h->geo[level];
         const size_t n = 3 * npts(g);
-        const double *src = which == STZ_MG_FIELD_X ? h->L64[level].x : h->L64[level].r;
+        const double *src = level_field(h, level, which);
         double *d = where == STZ_MG_DEVICE ? v : staging(h, n);
         launch_cb_to_nat<double>(g, src, d, h->st);
         check_launch();
         if (where != STZ_MG_DEVICE) CK(cudaMemcpyAsync(v, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_level_get_planes(stz_mg_handle h, int level, int which, int k0, int nk, double *v, int where) {
+    if (!h || !v) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        if (k0 < 0 || nk < 0 || k0 + nk > g.o) fail(STZ_MG_ERR_ARG, "planes %d..%d outside [0,%d)", k0, k0 + nk, g.o);
+        const double *src = level_field(h, level, which);
+        const size_t n = 3 * (size_t)g.m * g.n * nk;
+        if (n == 0) return;
+        if (where != STZ_MG_HOST && where != STZ_MG_DEVICE) fail(STZ_MG_ERR_ARG, "bad where");
+        double *d = where == STZ_MG_DEVICE ? v : staging(h, n);
+        const unsigned blocks = (unsigned)std::min<size_t>((n / 3 + 255) / 256, 152 * 8);
+        planes_cb_to_nat_kernel<<<blocks, 256, 0, h->st>>>(g, k0, nk, src, d);
+        check_launch();
+        if (where == STZ_MG_HOST) CK(cudaMemcpyAsync(v, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        sync(h);
+    });
+}
+
+int stz_mg_level_set_planes(stz_mg_handle h, int level, int which, int k0, int nk, const double *v, int where) {
+    if (!h || !v) return set_error(STZ_MG_ERR_ARG, "null argument");
+    return guarded(h, [&] {
+        check_level(h, level);
+        const Geom &g = h->geo[level];
+        if (k0 < 0 || nk < 0 || k0 + nk > g.o) fail(STZ_MG_ERR_ARG, "planes %d..%d outside [0,%d)", k0, k0 + nk, g.o);
+        double *dst = level_field(h, level, which);
+        const size_t n = 3 * (size_t)g.m * g.n * nk;
+        if (n == 0) return;
+        const double *src = to_device(h, v, n, where);
+        const unsigned blocks = (unsigned)std::min<size_t>((n / 3 + 255) / 256, 152 * 8);
+        planes_nat_to_cb_kernel<<<blocks, 256, 0, h->st>>>(g, k0, nk, src, dst);
+        check_launch();
+        if (level == 0 && which == STZ_MG_FIELD_R) h->bnorm = -1.0;
+        sync(h);
+    });
+}
+
+int stz_mg_level_gs_colours(stz_mg_handle h, int level, int q0, int q1) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        if (q0 < 0 || q1 > 8 || q0 > q1) fail(STZ_MG_ERR_ARG, "colours %d..%d outside [0,8)", q0, q1);
+        for (int q = q0; q < q1; q++)
+            launch_gs_colour<double>(h->op64[level], h->geo[level], q, h->L64[level].r, h->L64[level].x, h->st);
+        check_launch();
+        sync(h);
+    });
+}
+
+int stz_mg_level_restrict_residual(stz_mg_handle h, int level) {
+    if (!h) return set_error(STZ_MG_ERR_ARG, "null handle");
+    return guarded(h, [&] {
+        need_setup(h);
+        check_level(h, level);
+        if (level < 1) fail(STZ_MG_ERR_ARG, "restriction target must be a coarse level");
+        const int f = level - 1;
+        launch_restriction<double>(h->geo[f], h->geo[level], h->L64[f].res, h->L64[level].r, h->st);
+        CK(cudaMemsetAsync(h->L64[level].x, 0, 3 * (size_t)h->geo[level].npad * sizeof(double), h->st));
+        check_launch();
         sync(h);
     });
 }

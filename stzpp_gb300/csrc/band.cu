@@ -629,11 +629,16 @@ bool launch_band_persist(const LevelOp<T> &op, const Geom &g, const T *r, const 
     static unsigned long long attr_devices = 0;
     static int per_sm = 0, sms = 0;
     if (first_band_use(attr_devices)) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        int dev = 0;
+        int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NH * M2, smem);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        per_sm = 0;
+        // two staging buffers must fit one CTA's shared memory
+        if (smem <= optin && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NH * M2, smem) != cudaSuccess)
+            per_sm = 0;
+        cudaGetLastError();
     }
     if (per_sm < 1 || sms < 1) return false;
     BandArgs a;
@@ -655,7 +660,8 @@ template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
 bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     BandMaps min_, mout;
     if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
-    if (band_persist()) return launch_band_persist<T, M2, JOUT, KIND, SPARSE>(op, g, r, min_, mout, xout, st);
+    // the persistent form where its two buffers fit, else one CTA per item
+    if (band_persist() && launch_band_persist<T, M2, JOUT, KIND, SPARSE>(op, g, r, min_, mout, xout, st)) return true;
     constexpr int NH = kBandNH<T>;
     auto kern = gs_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);

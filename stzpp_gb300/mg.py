@@ -28,7 +28,8 @@ OK, ERR_ARG, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOCONV, ERR_SINGULAR, ERR_NONFINITE,
 FP64, MIXED = 0, 1
 BOTTOM_DIRECT, BOTTOM_GS = 0, 1
 HOST, DEVICE = 0, 1
-FIELD_X, FIELD_R = 0, 1
+FIELD_X, FIELD_R, FIELD_RES = 0, 1, 2
+_FIELDS = {"x": FIELD_X, "r": FIELD_R, "res": FIELD_RES}
 
 # every entry point declared in include/stz_mg.h
 EXPORTS = (
@@ -39,6 +40,7 @@ EXPORTS = (
     "stz_mg_solve_stats", "stz_mg_residual_norm", "stz_mg_l2_error_all", "stz_mg_num_levels", "stz_mg_level_dims",
     "stz_mg_level_operator", "stz_mg_level_set_field", "stz_mg_level_get_field",
     "stz_mg_level_gauss_seidel", "stz_mg_level_restriction", "stz_mg_level_interpolation",
+    "stz_mg_level_get_planes", "stz_mg_level_set_planes", "stz_mg_level_gs_colours", "stz_mg_level_restrict_residual",
     "stz_mg_level_residual", "stz_mg_time_kernel", "stz_mg_sweep_kind", "stz_mg_const_residual_sumsq_noalloc",
     "stz_mg_adjoint_solve", "stz_mg_coeff_grad", "stz_mg_stress_update", "stz_mg_advection_step",
     "stz_mg_output_slice", "stz_mg_cube_values", "stz_mg_output_cube",
@@ -98,6 +100,10 @@ def load_library():
     lib.stz_mg_level_get_field.argtypes = [vp, ci, ci, vp, ci]
     lib.stz_mg_level_gauss_seidel.argtypes = [vp, ci, ci]
     lib.stz_mg_level_restriction.argtypes = [vp, ci]
+    lib.stz_mg_level_get_planes.argtypes = [vp, ci, ci, ci, ci, vp, ci]
+    lib.stz_mg_level_set_planes.argtypes = [vp, ci, ci, ci, ci, vp, ci]
+    lib.stz_mg_level_gs_colours.argtypes = [vp, ci, ci, ci]
+    lib.stz_mg_level_restrict_residual.argtypes = [vp, ci]
     lib.stz_mg_level_interpolation.argtypes = [vp, ci]
     lib.stz_mg_level_residual.argtypes = [vp, ci, vp, ctypes.POINTER(cd), ci]
     lib.stz_mg_time_kernel.argtypes = [vp, ci, ci, ci, ctypes.POINTER(cd), ctypes.POINTER(cd)]
@@ -413,13 +419,39 @@ class Multigrid:
 
     def level_set_field(self, l, which, v):
         p, where, keep = _arg(v, 3 * self.level_npts(l))
-        _check(load_library().stz_mg_level_set_field(self._h, l, {"x": FIELD_X, "r": FIELD_R}[which], p, where))
+        _check(load_library().stz_mg_level_set_field(self._h, l, _FIELDS[which], p, where))
 
     def level_get_field(self, l, which):
         out = np.empty((self.level_npts(l), 3))
-        _check(load_library().stz_mg_level_get_field(self._h, l, {"x": FIELD_X, "r": FIELD_R}[which],
+        _check(load_library().stz_mg_level_get_field(self._h, l, _FIELDS[which],
                                                      out.ctypes.data_as(ctypes.c_void_p), HOST))
         return out
+
+    def level_get_planes(self, l, which, k0, nk, out=None):
+        """z-planes k0 .. k0+nk-1 of field `which` ("x", "r", "res") of level l,
+        (nk*m*n, 3) in natural order: a numpy array, or written into `out`
+        (a numpy array or a float64 CUDA tensor)."""
+        m, n, _ = self.level_dims(l)
+        if out is None:
+            out = np.empty((nk * m * n, 3))
+        p, where, keep = _arg(out, 3 * m * n * nk)
+        _check(load_library().stz_mg_level_get_planes(self._h, l, _FIELDS[which], k0, nk, p, where))
+        return out
+
+    def level_set_planes(self, l, which, k0, v):
+        """Set z-planes k0 .. of field `which` of level l from (nk*m*n, 3) values."""
+        m, n, _ = self.level_dims(l)
+        nk = (v.numel() if hasattr(v, "numel") else np.size(v)) // (3 * m * n)
+        p, where, keep = _arg(v, 3 * m * n * nk)
+        _check(load_library().stz_mg_level_set_planes(self._h, l, _FIELDS[which], k0, nk, p, where))
+
+    def gauss_seidel_colours(self, l, q0, q1):
+        """Colour passes q0 .. q1-1 of the 8-colour sweep of level l (FP64)."""
+        _check(load_library().stz_mg_level_gs_colours(self._h, l, q0, q1))
+
+    def restrict_residual(self, l):
+        """Coarse r of level l from the level-(l-1) residual field as it stands; coarse x = 0."""
+        _check(load_library().stz_mg_level_restrict_residual(self._h, l))
 
     def gauss_seidel(self, l, sweeps=1):
         _check(load_library().stz_mg_level_gauss_seidel(self._h, l, sweeps))
@@ -429,6 +461,13 @@ class Multigrid:
 
     def interpolation(self, l):
         _check(load_library().stz_mg_level_interpolation(self._h, l))
+
+    def compute_residual(self, l=0):
+        """r - A x of level l into its residual field (STZ_MG_FIELD_RES),
+        nothing copied out; returns |r - A x|^2."""
+        sq = ctypes.c_double()
+        _check(load_library().stz_mg_level_residual(self._h, l, None, ctypes.byref(sq), HOST))
+        return sq.value
 
     def residual(self, l=0):
         out = np.empty((self.level_npts(l), 3))
