@@ -124,6 +124,7 @@ struct BandArgs {
     int nbands;     // n / kBandRows
     int nplanes;    // planes of parity c
     int rev;        // planes taken from the top down
+    const void *xz; // the residual's x (read directly on Dirichlet plates)
 };
 
 // Stage plane kk of a field (three components) into buffer plane p: boxes
@@ -522,6 +523,158 @@ __global__ void __launch_bounds__(NH * M2, 1)
     }
 }
 
+// ------------------------------------------------------------ residual
+// res = r - A x on one band of plane k: the same staging, every colour on the
+// band's own rows (no chain between colours, so no halo row and no barrier
+// between them), in the arithmetic and order of residual_kernel
+// (const_row<T, ELASTIC, true> / plane_row_coef<T, SPARSE, true>).
+template <typename T, int M2, bool JOUT, int KIND, bool SPARSE, int A, int B, int NR>
+__device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const int (&ib)[3], const LevelOp<T> &op,
+                                                const T *cf, int t0, int nv, const Geom &g, int c, int K, int J0,
+                                                int I, const T *__restrict__ r, T *__restrict__ res) {
+    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    const size_t np = (size_t)g.npad;
+#pragma unroll 1
+    for (int u = 0; u < NR; u++) {
+        if (u >= nv) break;
+        const int t = t0 + u, Jr = t + 1;
+        const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
+        T acc[3] = {r[sl], r[sl + np], r[sl + 2 * np]};
+        if constexpr (KIND == OP_CONST) {
+            T v[27][3];
+            sfor<0, 27>([&](auto bi) {
+                constexpr int b = decltype(bi)::value;
+                if constexpr (nnz_axes(b) != 3) {
+                    constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+                    constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+                    constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+                    sfor<0, 3>([&](auto ci) {
+                        constexpr int cc = decltype(ci)::value;
+                        constexpr bool used =
+                            b == 13 || elastic_entry(b, cc) || elastic_entry(b, 3 + cc) || elastic_entry(b, 6 + cc);
+                        if constexpr (used) v[b][cc] = s[ib[sI + 1] + woff<M2, JOUT>(1 + dz, cc, 0, ap + 2 * bp, 0) +
+                                                         (Jr + sJ) * rowstep];
+                        else v[b][cc] = T(0);
+                    });
+                }
+            });
+#pragma unroll
+            for (int b = 0; b < 27; b++) {
+                if (nnz_axes(b) == 3) continue;
+                if (b != 13) {
+#pragma unroll
+                    for (int e = 0; e < 9; e++)
+                        if (elastic_entry(b, e)) acc[e / 3] -= op.cop.a[b][e] * v[b][e % 3];
+                } else if (op.cop.centre_diag) {
+                    acc[0] -= op.cop.a[13][0] * v[13][0];
+                    acc[1] -= op.cop.a[13][4] * v[13][1];
+                    acc[2] -= op.cop.a[13][8] * v[13][2];
+                } else {
+                    matvec_sub(op.cop.a[13], v[13], acc);
+                }
+            }
+        } else {
+            // one block at a time (its three values, then its products in
+            // plane_row_coef's order): a whole row would not fit in registers
+            sfor<0, 27>([&](auto bi) {
+                constexpr int b = decltype(bi)::value;
+                constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+                constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+                constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+                asm volatile("" ::: "memory");
+                const int base = ib[sI + 1] + (Jr + sJ) * rowstep;
+                T v[3];
+                v[0] = s[base + woff<M2, JOUT>(1 + dz, 0, 0, ap + 2 * bp, 0)];
+                v[1] = s[base + woff<M2, JOUT>(1 + dz, 1, 0, ap + 2 * bp, 0)];
+                v[2] = s[base + woff<M2, JOUT>(1 + dz, 2, 0, ap + 2 * bp, 0)];
+#pragma unroll
+                for (int e = 0; e < 9; e++)
+                    if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[9 * b + e] * v[e % 3];
+            });
+        }
+        res[sl] = acc[0];
+        res[sl + np] = acc[1];
+        res[sl + 2 * np] = acc[2];
+    }
+}
+
+template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+__global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
+    residual_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op,
+                         const __grid_constant__ BandMaps xm, const T *__restrict__ r, T *__restrict__ res) {
+    extern __shared__ __align__(128) unsigned char band_smem[];
+    __shared__ __align__(8) unsigned long long bar_store;
+    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+    const Geom &g = args.g;
+    const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
+    const int band = blockIdx.x % args.nbands, k = blockIdx.x / args.nbands;
+    const int c = k & 1, K = k >> 1, J0 = band * kOwnSub;
+    const size_t np = (size_t)g.npad;
+    const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
+    if (KIND == OP_CONST && !(has_lo && has_hi)) {   // a Dirichlet plate: r - fix x
+#pragma unroll 1
+        for (int w = hh; w < 4 * kOwnSub; w += NH) {
+            const int ab = w / kOwnSub, t = w % kOwnSub;
+            const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
+            T acc[3] = {r[sl], r[sl + np], r[sl + 2 * np]};
+            const T *xp = static_cast<const T *>(args.xz);
+            const T v[3] = {xp[sl], xp[sl + np], xp[sl + 2 * np]};
+            matvec_sub(op.cop.fix, v, acc);
+            res[sl] = acc[0];
+            res[sl + np] = acc[1];
+            res[sl + 2 * np] = acc[2];
+        }
+        return;
+    }
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&bar_store);
+    if ((sbase & 127u) != 0) {
+        if (tid == 0) atomicExch(&g_band_err, 2);
+        return;
+    }
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned plane_bytes = (unsigned)(kBandWords<M2> / 3 * sizeof(T));
+        mbar_expect_tx(bar, plane_bytes * (1u + has_lo + has_hi));
+        const int klo = k == 0 ? g.o - 1 : k - 1, khi = k == g.o - 1 ? 0 : k + 1;
+        if (has_lo) stage_plane<T, M2, JOUT>(xm, g, klo, J0, 0, sbase, bar);
+        stage_plane<T, M2, JOUT>(xm, g, k, J0, 1, sbase, bar);
+        if (has_hi) stage_plane<T, M2, JOUT>(xm, g, khi, J0, 2, sbase, bar);
+    }
+    if (KIND == OP_PLANE)
+        for (int e = tid; e < 252; e += NH * M2)
+            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+    const bool ok = mbar_wait(bar, 0, 200000000ull);
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) {
+            atomicExch(&g_band_err, 1);
+            mbar_wait(bar, 0, 200000000ull);
+        }
+        __syncthreads();
+        return;
+    }
+    T *s = reinterpret_cast<T *>(band_smem);
+    if (KIND == OP_PLANE && !(has_lo && has_hi)) {
+        constexpr int PW = kBandWords<M2> / 3;
+        if (!has_lo)
+            for (int w = tid; w < PW; w += NH * M2) s[w] = T(0);
+        if (!has_hi)
+            for (int w = tid; w < PW; w += NH * M2) s[2 * PW + w] = T(0);
+        __syncthreads();
+    }
+    constexpr int P = kPer<kOwnSub, NH>;
+    const int t0 = hh * P, nv = min(P, kOwnSub - t0);
+    const int ib[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
+    band_res_colour<T, M2, JOUT, KIND, SPARSE, 0, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+    band_res_colour<T, M2, JOUT, KIND, SPARSE, 1, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+    band_res_colour<T, M2, JOUT, KIND, SPARSE, 0, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+    band_res_colour<T, M2, JOUT, KIND, SPARSE, 1, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+}
+
 // ------------------------------------------------------------------ host
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -609,10 +762,12 @@ bool first_band_use(unsigned long long &devices) {
     return true;
 }
 
-// Threads per column of the band kernel: two in FP32 (twice the warps for
-// the same shared memory), one in FP64 (one CTA per SM, registers)
-template <typename T>
-constexpr int kBandNH = sizeof(T) == 4 ? 2 : 1;
+// Threads per column of the band kernel: two on wide FP32 levels (twice the
+// warps for the same shared memory), four on narrow ones (a level of 8-32
+// sub-grid columns has few nodes per row), one or two in FP64 (shared
+// memory and registers)
+template <typename T, int M2>
+constexpr int kBandNH = sizeof(T) == 4 ? (M2 >= 64 ? 2 : 4) : (M2 >= 64 ? 1 : 2);
 
 // The persistent double-buffered form (STZ_MG_BAND_PERSIST=1) or one CTA per item.
 bool band_persist() {
@@ -662,7 +817,7 @@ bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin
     if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
     // the persistent form where its two buffers fit, else one CTA per item
     if (band_persist() && launch_band_persist<T, M2, JOUT, KIND, SPARSE>(op, g, r, min_, mout, xout, st)) return true;
-    constexpr int NH = kBandNH<T>;
+    constexpr int NH = kBandNH<T, M2>;
     auto kern = gs_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);
     static unsigned long long attr_devices = 0;
@@ -687,6 +842,8 @@ bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin
 template <typename T, bool JOUT, int KIND, bool SPARSE>
 bool launch_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     switch (g.M2) {
+        case 8: return launch_band_k<T, 8, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 16: return launch_band_k<T, 16, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
         case 32: return launch_band_k<T, 32, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
         case 64: return launch_band_k<T, 64, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
         case 128: return launch_band_k<T, 128, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
@@ -704,9 +861,9 @@ bool launch_band_op(const LevelOp<T> &op, const Geom &g, const T *r, const T *xi
 }  // namespace
 
 // Where the band sweep runs: the elasticity stencil shared by every interior
-// node, a level periodic in x and y with an even number of columns in 32,
-// 64 or 128 sub-grid columns (64 .. 256 nodes) and whole bands of 8 rows (at
-// least two), an even z extent if z is periodic.  FP32 levels by default;
+// node or a plane-invariant coarse operator, a level periodic in x and y
+// with 8, 16, 32, 64 or 128 sub-grid columns (16 .. 256 nodes) and whole
+// bands of 8 rows (at least two), an even z extent if z is periodic.  FP32 levels by default;
 // STZ_MG_BAND=0 turns it off, STZ_MG_BAND=1 uses it in FP64 too.
 template <typename T>
 bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
@@ -716,7 +873,7 @@ bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
     if (mode < 0 && sizeof(T) != 4) return false;
     if (!((op.kind == OP_CONST && op.cop.elastic) || op.kind == OP_PLANE)) return false;
     if (!g.xp || !g.yp || (g.m & 1) || g.n % kBandRows != 0 || g.n < 2 * kBandRows) return false;
-    if (g.M2 != 32 && g.M2 != 64 && g.M2 != 128) return false;
+    if (g.M2 != 8 && g.M2 != 16 && g.M2 != 32 && g.M2 != 64 && g.M2 != 128) return false;
     if (g.zp && (g.o & 1)) return false;
     return true;
 }
@@ -730,6 +887,64 @@ bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const
     if (layout == 0) return launch_band_op<T, false>(op, g, r, xin, xout, st);
     return false;
 }
+
+namespace {
+
+template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
+bool launch_res_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
+    BandMaps xm;
+    if (!make_band_maps<T, JOUT>(g, x, xm)) return false;
+    constexpr int NH = kBandNH<T, M2>;
+    auto kern = residual_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
+    const int smem = kBandWords<M2> * (int)sizeof(T);
+    static unsigned long long attr_devices = 0;
+    if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    BandArgs a;
+    a.g = g;
+    a.nbands = g.n / kBandRows;
+    a.c = 0;
+    a.nplanes = g.o;
+    a.rev = 0;
+    a.xz = x;
+    kern<<<a.nbands * g.o, NH * M2, smem, st>>>(a, op, xm, r, res);
+    return true;
+}
+
+template <typename T, bool JOUT, int KIND, bool SPARSE>
+bool launch_res_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
+    switch (g.M2) {
+        case 8: return launch_res_band_k<T, 8, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        case 16: return launch_res_band_k<T, 16, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        case 32: return launch_res_band_k<T, 32, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        case 64: return launch_res_band_k<T, 64, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        case 128: return launch_res_band_k<T, 128, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        default: return false;
+    }
+}
+
+template <typename T, bool JOUT>
+bool launch_res_band_op(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
+    if (op.kind == OP_CONST) return launch_res_band_m<T, JOUT, OP_CONST, false>(op, g, r, x, res, st);
+    if (op.pop.sparse) return launch_res_band_m<T, JOUT, OP_PLANE, true>(op, g, r, x, res, st);
+    return launch_res_band_m<T, JOUT, OP_PLANE, false>(op, g, r, x, res, st);
+}
+
+}  // namespace
+
+// res = r - A x by the band kernel where the band sweep applies; false (the
+// caller falls back) where it does not or the tensor maps cannot be made.
+template <typename T>
+bool launch_residual_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
+    if (!gs_band_applies(op, g)) return false;
+    const int layout = band_layout<T>(g, x);
+    if (layout == 1) return launch_res_band_op<T, true>(op, g, r, x, res, st);
+    if (layout == 0) return launch_res_band_op<T, false>(op, g, r, x, res, st);
+    return false;
+}
+template bool launch_residual_band<float>(const LevelOp<float> &, const Geom &, const float *, const float *, float *,
+                                          cudaStream_t);
+template bool launch_residual_band<double>(const LevelOp<double> &, const Geom &, const double *, const double *,
+                                           double *, cudaStream_t);
 
 // Whether the tensor maps of the band sweep can be made for this level.
 template <typename T>

@@ -43,6 +43,10 @@ template <typename T>
 bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st);
 template <typename T>
 bool gs_band_ready(const Geom &g, const T *field);
+// band.cu: res = r - A x by full-width bands staged by TMA where the band
+// sweep applies (no norm); false where it does not
+template <typename T>
+bool launch_residual_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st);
 // How launch_gs_sweeps smooths a level: 0 eight colour launches per sweep,
 // 1 the tiled two-buffer sweep, 2 the band sweep, 3 the plane-phase kernels
 // (two launches per sweep each but the first)

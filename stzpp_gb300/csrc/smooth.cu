@@ -412,6 +412,11 @@ static void launch_residual_k(const LevelOp<T> &op, const Geom &g, const T *r, c
 template <typename T, typename R>
 void launch_residual(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, R *res, double *partial,
                      double *out, cudaStream_t st) {
+    if constexpr (std::is_same<T, R>::value) {
+        // the band kernel on the levels the band sweep serves (no norm there)
+        if (res && !partial && launch_residual_band<T>(op, g, r, x, reinterpret_cast<T *>(res), st))
+            return;
+    }
     if (std::is_same<T, R>::value && res && residual_tile_applies(op, g)) {
         launch_residual_tile<T>(op, g, r, x, reinterpret_cast<T *>(res), partial, st);
         if (partial && out) sum_partials_kernel<<<1, 1024, 0, st>>>(partial, residual_tile_blocks(g, sizeof(T) == 8), out);

@@ -172,6 +172,29 @@ struct Stager {
 // then the products.  WITH_CENTRE: include the centre block (residual).
 template <typename T, bool ELASTIC, bool WITH_CENTRE, int A, int NROWS>
 __device__ __forceinline__ void tile_const_row(const ConstOp<T> &op, const unsigned (&cz)[3], T *acc) {
+    if constexpr (!ELASTIC) {
+        // a full-block stencil: each block's three values right before its
+        // products (the same products in the same order; 81 values at once
+        // would spill)
+        static_for<0, 27>([&](auto bi) {
+            constexpr int b = decltype(bi)::value;
+            if constexpr (b != 13 || WITH_CENTRE) {
+                asm volatile("" ::: "memory");
+                T v[3];
+                lds<nb_off<A, NROWS>(b, 0)>(cz[bdz(b) + 1], v[0]);
+                lds<nb_off<A, NROWS>(b, 1)>(cz[bdz(b) + 1], v[1]);
+                lds<nb_off<A, NROWS>(b, 2)>(cz[bdz(b) + 1], v[2]);
+                if (b == 13 && op.centre_diag) {
+                    acc[0] -= op.a[13][0] * v[0];
+                    acc[1] -= op.a[13][4] * v[1];
+                    acc[2] -= op.a[13][8] * v[2];
+                } else {
+                    matvec_sub(op.a[b], v, acc);
+                }
+            }
+        });
+        return;
+    }
     T v[27][3];
     static_for<0, 27>([&](auto bi) {
         constexpr int b = decltype(bi)::value;

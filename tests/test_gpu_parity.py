@@ -326,7 +326,9 @@ BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64
                     ((128, 64, 9), (True, True, False), "const", 0, 3), ((128, 128, 8), (True, True, True), "const", 0, 2),
                     ((256, 256, 9), (True, True, False), "const", 0, 2), ((64, 16, 5), (True, True, False), "const", 0, 4),
                     ((128, 128, 17), (True, True, False), "const", 1, 2), ((128, 128, 16), (True, True, True), "const", 1, 3),
-                    ((128, 64, 17), (True, True, False), "trans", 1, 2), ((256, 128, 10), (True, True, False), "trans", 1, 2)]
+                    ((128, 64, 17), (True, True, False), "trans", 1, 2), ((256, 128, 10), (True, True, False), "trans", 1, 2),
+                    ((32, 32, 17), (True, True, False), "const", 0, 2), ((16, 16, 9), (True, True, False), "const", 0, 3),
+                    ((64, 64, 33), (True, True, False), "const", 1, 2), ((64, 32, 16), (True, True, True), "trans", 1, 2)]
 
 
 @pytest.mark.parametrize("persist", ["0", "1"])
@@ -438,3 +440,27 @@ def test_fourier_bottom_inverse_is_the_dense_inverse(dims, kind, precision, monk
     assert out["0"][0] == out["1"][0]
     x0, x1 = out["0"][1], out["1"][1]
     assert np.linalg.norm(x1 - x0) <= 1e-11 * np.linalg.norm(x0)
+
+
+@pytest.mark.parametrize("dims,per,kind", [((128, 128, 33), (True, True, False), "const"),
+                                          ((128, 64, 24), (True, True, False), "trans"),
+                                          ((64, 64, 32), (True, True, False), "const")])
+def test_band_kernels_fp64_solve_bitwise(dims, per, kind, monkeypatch):
+    """FP64 solves with the band kernels forced (STZ_MG_BAND=1: the band sweep
+    and the band residual on every level they serve) and without: the same
+    cycle count and the same solution bit for bit."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per, h=1.0 / m)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(1, h[0])
+    out = {}
+    for band in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_BAND", band)
+        with sg.Multigrid(dims, per, precision="fp64", sweep_growth=False, v_down=2, v_up=2) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-10, 6, check=False)
+            out[band] = (cyc, rel, mg.get_x())
+    assert out["0"][:2] == out["1"][:2]
+    assert np.array_equal(out["0"][2], out["1"][2])
