@@ -350,13 +350,18 @@ def run_ours(args, world, rank, local):
     b_host.copy_(b_dev)
     x_host = torch.empty(3 * npts, dtype=torch.float64, pin_memory=True)
     e2e_steps = max(2, args.steps // 2)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         mg.set_rhs(b_host)          # host -> device
         mg.set_x(zero)
         mg.solve(TOL, 200)
         mg.get_x(x_host)            # device -> host
+
+    e2e_step()   # untimed: the first copies into freshly pinned pages map them
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     barrier()
     ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps)
 

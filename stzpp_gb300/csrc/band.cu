@@ -51,12 +51,11 @@ constexpr int kStageRows = kOwnSub + 2;    // staged sub-rows J0-1 .. J0+kOwnSub
 
 // Shared-memory layout of the staged band: plane p (0: k-1, 1: k, 2: k+1),
 // component c, sub-row Jr (staged row 0 is sub-row J0-1), colour ab = a + 2b
-// of the plane, sub-grid column I.  JOUT: Jr outside ab (one TMA box per
-// plane and component); otherwise ab outside Jr (one box per colour).
-template <int M2, bool JOUT>
+// of the plane, sub-grid column I: Jr outside ab, so one TMA box brings a
+// plane's component (all four colours of the staged sub-rows).
+template <int M2>
 __host__ __device__ constexpr int woff(int p, int c, int Jr, int ab, int I) {
-    return JOUT ? (((p * 3 + c) * kStageRows + Jr) * 4 + ab) * M2 + I
-                : (((p * 3 + c) * 4 + ab) * kStageRows + Jr) * M2 + I;
+    return (((p * 3 + c) * kStageRows + Jr) * 4 + ab) * M2 + I;
 }
 template <int M2>
 constexpr int kBandWords = 3 * 3 * kStageRows * 4 * M2;
@@ -130,31 +129,61 @@ struct BandArgs {
 // Stage plane kk of a field (three components) into buffer plane p: boxes
 // cover sub-rows J0-1 .. J0+kOwnSub, split where they cross the periodic
 // wrap in y.  Every plane delivers a third of kBandWords<M2> elements.
-template <typename T, int M2, bool JOUT>
+template <typename T, int M2>
 __device__ __forceinline__ void stage_plane(const BandMaps &mp, const Geom &g, int kk, int J0, int p,
                                                 unsigned sbase, unsigned bar) {
     const int K = kk >> 1, cpar = kk & 1;
-    constexpr unsigned rowb = (JOUT ? 4 * M2 : M2) * sizeof(T);   // bytes per staged sub-row of one box
-    const int nab = JOUT ? 1 : 4;
-    for (int comp = 0; comp < 3; comp++)
-        for (int ab = 0; ab < nab; ab++) {
-            const unsigned dst = sbase + (unsigned)(woff<M2, JOUT>(p, comp, 0, ab, 0) * (int)sizeof(T));
-            const int cc = 2 * comp + cpar;
-            // coordinates: JOUT (I, ab, J, K, cc), else (I, J, K, ab, cc)
-            auto load = [&](const CUtensorMap *map, int J, unsigned d) {
-                if (JOUT) tma_load5(d, map, 0, 0, J, K, cc, bar);
-                else tma_load5(d, map, 0, J, K, ab, cc, bar);
-            };
-            if (J0 == 0) {   // rows N2-1 | 0 .. kOwnSub
-                load(&mp.rows1, g.N2 - 1, dst);
-                load(&mp.rows5, 0, dst + rowb);
-            } else if (J0 + kOwnSub == g.N2) {   // rows J0-1 .. N2-1 | 0
-                load(&mp.rows5, J0 - 1, dst);
-                load(&mp.rows1, 0, dst + 5 * rowb);
-            } else {
-                load(&mp.rows6, J0 - 1, dst);
-            }
+    constexpr unsigned rowb = 4 * M2 * sizeof(T);   // bytes per staged sub-row (four colours)
+    for (int comp = 0; comp < 3; comp++) {
+        const unsigned dst = sbase + (unsigned)(woff<M2>(p, comp, 0, 0, 0) * (int)sizeof(T));
+        const int cc = 2 * comp + cpar;
+        // coordinates (I, ab, J, K, cc)
+        if (J0 == 0) {   // rows N2-1 | 0 .. kOwnSub
+            tma_load5(dst, &mp.rows1, 0, 0, g.N2 - 1, K, cc, bar);
+            tma_load5(dst + rowb, &mp.rows5, 0, 0, 0, K, cc, bar);
+        } else if (J0 + kOwnSub == g.N2) {   // rows J0-1 .. N2-1 | 0
+            tma_load5(dst, &mp.rows5, 0, 0, J0 - 1, K, cc, bar);
+            tma_load5(dst + 5 * rowb, &mp.rows1, 0, 0, 0, K, cc, bar);
+        } else {
+            tma_load5(dst, &mp.rows6, 0, 0, J0 - 1, K, cc, bar);
         }
+    }
+}
+
+// Plane k's coarse row in shared memory: block b's 9 coefficients at
+// kCoefPad * b (padded to 16-byte boundaries), the inverse centre block at
+// kCoefPad * 27.
+constexpr int kCoefPad = 12;
+constexpr int kCoefWords = kCoefPad * 28;
+
+// The 9 entries of one padded block (the 16-byte loads cover 12).
+template <typename T>
+__device__ __forceinline__ void load_block_coef(const T *p, T (&c)[kCoefPad]) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float4 w = q[i];
+            c[4 * i] = w.x; c[4 * i + 1] = w.y; c[4 * i + 2] = w.z; c[4 * i + 3] = w.w;
+        }
+    } else {
+        const double2 *q = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+            const double2 w = q[i];
+            c[2 * i] = w.x; c[2 * i + 1] = w.y;
+        }
+        c[10] = c[11] = T(0);
+    }
+}
+
+// Plane k's row into the padded shared layout (all threads of the CTA).
+template <typename T>
+__device__ __forceinline__ void stage_coef(const PlaneOp<T> &pop, int k, T *cfs, int tid, int nthreads) {
+    for (int e = tid; e < 252; e += nthreads) {
+        const int b = e / 9, i = e % 9;
+        cfs[kCoefPad * b + i] = e < 243 ? pop.coef[e * pop.O + k] : pop.dinv[(e - 243) * pop.O + k];
+    }
 }
 
 // One colour (A, B) of plane k (buffer plane 1) on up to NR sub-rows
@@ -170,41 +199,57 @@ __device__ __forceinline__ void stage_plane(const BandMaps &mp, const Geom &g, i
 // of the inverse centre block, in shared memory; SPARSE: the structural
 // zeros of the coarse elasticity operators), with the arithmetic of
 // const_row<T, true, false> or plane_row_coef<T, SPARSE, false>.
-template <typename T, int M2, bool JOUT, int KIND, bool SPARSE, int A, int B, int NR>
+template <typename T, int M2, int KIND, bool SPARSE, int A, int B, int NR>
 __device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (&ib)[3], const LevelOp<T> &op,
                                             const T *cf, int nvalid, const T (&rr)[NR][3], T (&out)[NR][3]) {
     constexpr bool CONST = KIND == OP_CONST;
-    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    constexpr int rowstep = woff<M2>(0, 0, 1, 0, 0);
     if constexpr (!CONST) {
-        // a full coarse row: one block at a time (its three neighbour values,
-        // then its products), as plane_row_coef orders the products; all 78
-        // values at once would not fit in registers (nor would several rows)
-#pragma unroll 1
-        for (int u = 0; u < NR; u++) {
-            if (u >= nvalid) break;   // warp-uniform
-            const int Jr = u + 1;
-            T acc[3] = {rr[u][0], rr[u][1], rr[u][2]};
-            sfor<0, 27>([&](auto bi) {
-                constexpr int b = decltype(bi)::value;
-                if constexpr (b != 13) {
-                    constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
-                    constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
-                    constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
-                    asm volatile("" ::: "memory");
-                    const int base = ib[sI + 1] + (Jr + sJ) * rowstep;
+        // plane k's coarse row, one block at a time: its 9 coefficients
+        // (16-byte shared loads of the padded row, the same for every thread)
+        // serve all of this thread's rows, then each row takes its three
+        // neighbour values and its products in plane_row_coef's order
+        if (nvalid <= 0) return;
+        // rows past this thread's last repeat its last row (no branch inside
+        // the block loop; their results are not stored)
+        int roff[NR];
+#pragma unroll
+        for (int u = 0; u < NR; u++) roff[u] = (1 + min(u, nvalid - 1)) * rowstep;
+        T acc[NR][3];
+#pragma unroll
+        for (int u = 0; u < NR; u++)
+#pragma unroll
+            for (int e = 0; e < 3; e++) acc[u][e] = rr[u][e];
+        sfor<0, 27>([&](auto bi) {
+            constexpr int b = decltype(bi)::value;
+            if constexpr (b != 13) {
+                constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+                constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+                constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+                asm volatile("" ::: "memory");
+                T cb[kCoefPad];
+                load_block_coef<T>(cf + kCoefPad * b, cb);
+#pragma unroll
+                for (int u = 0; u < NR; u++) {
+                    const int base = ib[sI + 1] + roff[u] + sJ * rowstep;
                     T v[3];
-                    v[0] = s[base + woff<M2, JOUT>(1 + dz, 0, 0, ap + 2 * bp, 0)];
-                    v[1] = s[base + woff<M2, JOUT>(1 + dz, 1, 0, ap + 2 * bp, 0)];
-                    v[2] = s[base + woff<M2, JOUT>(1 + dz, 2, 0, ap + 2 * bp, 0)];
+                    v[0] = s[base + woff<M2>(1 + dz, 0, 0, ap + 2 * bp, 0)];
+                    v[1] = s[base + woff<M2>(1 + dz, 1, 0, ap + 2 * bp, 0)];
+                    v[2] = s[base + woff<M2>(1 + dz, 2, 0, ap + 2 * bp, 0)];
 #pragma unroll
                     for (int e = 0; e < 9; e++)
-                        if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[9 * b + e] * v[e % 3];
+                        if (!SPARSE || coarse_entry(b, e)) acc[u][e / 3] -= cb[e] * v[e % 3];
                 }
-            });
-            const T *inv = cf + 243;
-            out[u][0] = dot3(inv[0], acc[0], inv[1], acc[1], inv[2], acc[2]);
-            out[u][1] = dot3(inv[3], acc[0], inv[4], acc[1], inv[5], acc[2]);
-            out[u][2] = dot3(inv[6], acc[0], inv[7], acc[1], inv[8], acc[2]);
+            }
+        });
+        T inv[kCoefPad];
+        load_block_coef<T>(cf + kCoefPad * 27, inv);
+#pragma unroll
+        for (int u = 0; u < NR; u++) {
+            if (u >= nvalid) break;
+            out[u][0] = dot3(inv[0], acc[u][0], inv[1], acc[u][1], inv[2], acc[u][2]);
+            out[u][1] = dot3(inv[3], acc[u][0], inv[4], acc[u][1], inv[5], acc[u][2]);
+            out[u][2] = dot3(inv[6], acc[u][0], inv[7], acc[u][1], inv[8], acc[u][2]);
         }
         return;
     }
@@ -222,8 +267,8 @@ __device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (
                 sfor<0, 3>([&](auto ci) {
                     constexpr int c = decltype(ci)::value;
                     constexpr bool used = elastic_entry(b, c) || elastic_entry(b, 3 + c) || elastic_entry(b, 6 + c);
-                    if constexpr (used) v[b][c] = s[ib[sI + 1] + woff<M2, JOUT>(1 + dz, c, 0, ap + 2 * bp, 0) +
-                                                    (Jr + sJ) * woff<M2, JOUT>(0, 0, 1, 0, 0)];
+                    if constexpr (used) v[b][c] = s[ib[sI + 1] + woff<M2>(1 + dz, c, 0, ap + 2 * bp, 0) +
+                                                    (Jr + sJ) * woff<M2>(0, 0, 1, 0, 0)];
                     else v[b][c] = T(0);
                 });
             }
@@ -283,7 +328,7 @@ __device__ __forceinline__ bool band_stages(const BandItem &it) {
 
 // Thread 0: the boxes of an item's planes into the buffer at sbuf,
 // completing on bar (every byte announced before any box is issued).
-template <typename T, int M2, bool JOUT>
+template <typename T, int M2>
 __device__ __forceinline__ void band_issue(const BandArgs &args, const BandMaps &in, const BandMaps &out_maps,
                                            const BandItem &it, unsigned sbuf, unsigned bar) {
     const Geom &g = args.g;
@@ -293,9 +338,9 @@ __device__ __forceinline__ void band_issue(const BandArgs &args, const BandMaps 
     // ones (x_out) under the odd launch; plane k itself from x_in
     const BandMaps &zm = args.c == 0 ? in : out_maps;
     const int klo = it.k == 0 ? g.o - 1 : it.k - 1, khi = it.k == g.o - 1 ? 0 : it.k + 1;
-    if (it.has_lo) stage_plane<T, M2, JOUT>(zm, g, klo, it.J0, 0, sbuf, bar);
-    stage_plane<T, M2, JOUT>(in, g, it.k, it.J0, 1, sbuf, bar);
-    if (it.has_hi) stage_plane<T, M2, JOUT>(zm, g, khi, it.J0, 2, sbuf, bar);
+    if (it.has_lo) stage_plane<T, M2>(zm, g, klo, it.J0, 0, sbuf, bar);
+    stage_plane<T, M2>(in, g, it.k, it.J0, 1, sbuf, bar);
+    if (it.has_hi) stage_plane<T, M2>(zm, g, khi, it.J0, 2, sbuf, bar);
 }
 
 // A Dirichlet plate of the shared stencil: x = fix^-1 r, no neighbours.
@@ -320,7 +365,7 @@ __device__ __forceinline__ void band_plate(const Geom &g, const ConstOp<T> &op, 
 // boxes are in flight), the wait for the boxes (phase `phase` of bar, at
 // most 0.2 s), then the plane's four colours.  False if the boxes did not
 // arrive (recorded; every thread returns false).
-template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+template <typename T, int M2, int NH, int KIND, bool SPARSE>
 __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp<T> &op, const BandItem &it, T *s,
                                              T *cfs, unsigned bar, unsigned phase, const T *__restrict__ r,
                                              T *__restrict__ xout) {
@@ -340,8 +385,8 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
         const size_t s0 = band_slot(g, 0, c, K, J, I), s1 = band_slot(g, 1, c, K, J, I);
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
-            r0[u][cc] = r[s0 + cc * np];
-            r1[u][cc] = r[s1 + cc * np];
+            r0[u][cc] = __ldcs(r + s0 + cc * np);
+            r1[u][cc] = __ldcs(r + s1 + cc * np);
         }
     }
 #pragma unroll
@@ -350,13 +395,11 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
         const size_t s2 = band_slot(g, 2, c, K, J0 + t0b + u, I), s3 = band_slot(g, 3, c, K, J0 + t0b + u, I);
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
-            r2[u][cc] = r[s2 + cc * np];
-            r3[u][cc] = r[s3 + cc * np];
+            r2[u][cc] = __ldcs(r + s2 + cc * np);
+            r3[u][cc] = __ldcs(r + s3 + cc * np);
         }
     }
-    if (KIND == OP_PLANE)   // plane k's row of coefficients
-        for (int e = tid; e < 252; e += NH * M2)
-            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+    if (KIND == OP_PLANE) stage_coef<T>(op.pop, k, cfs, tid, NH * M2);   // plane k's row of coefficients
     const bool ok = mbar_wait(bar, phase, 200000000ull);   // 0.2 s: copies that never arrive
     if (!__syncthreads_and(ok)) {
         if (tid == 0) {
@@ -376,7 +419,7 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
             for (int w = tid; w < PW; w += NH * M2) s[2 * PW + w] = T(0);
         __syncthreads();
     }
-    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    constexpr int rowstep = woff<M2>(0, 0, 1, 0, 0);
     const int ibx[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
     const int iba[3] = {ibx[0] + t0a * rowstep, ibx[1] + t0a * rowstep, ibx[2] + t0a * rowstep};
     const int ibb[3] = {ibx[0] + t0b * rowstep, ibx[1] + t0b * rowstep, ibx[2] + t0b * rowstep};
@@ -390,7 +433,7 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
             const int t = t0 + u;
             if (to_smem)
 #pragma unroll
-                for (int cc = 0; cc < 3; cc++) s[I + woff<M2, JOUT>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[u][cc];
+                for (int cc = 0; cc < 3; cc++) s[I + woff<M2>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[u][cc];
             if (t < kOwnSub) {
                 const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
 #pragma unroll
@@ -404,38 +447,38 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
     using NR1 = std::integral_constant<int, P1>;
     {
         T o[P0][3];
-        band_colour<T, M2, JOUT, KIND, SPARSE, 0, 0, P0>(s, iba, op, cfs, na, r0, o);
+        band_colour<T, M2, KIND, SPARSE, 0, 0, P0>(s, iba, op, cfs, na, r0, o);
         emit(I0{}, I0{}, NR0{}, t0a, na, o, true);
     }
     __syncthreads();
     {
         T o[P0][3];
-        band_colour<T, M2, JOUT, KIND, SPARSE, 1, 0, P0>(s, iba, op, cfs, na, r1, o);
+        band_colour<T, M2, KIND, SPARSE, 1, 0, P0>(s, iba, op, cfs, na, r1, o);
         emit(I1{}, I0{}, NR0{}, t0a, na, o, true);
     }
     __syncthreads();
     {
         T o[P1][3];
-        band_colour<T, M2, JOUT, KIND, SPARSE, 0, 1, P1>(s, ibb, op, cfs, nb, r2, o);
+        band_colour<T, M2, KIND, SPARSE, 0, 1, P1>(s, ibb, op, cfs, nb, r2, o);
         emit(I0{}, I1{}, NR1{}, t0b, nb, o, true);
     }
     __syncthreads();
     {
         T o[P1][3];
-        band_colour<T, M2, JOUT, KIND, SPARSE, 1, 1, P1>(s, ibb, op, cfs, nb, r3, o);
+        band_colour<T, M2, KIND, SPARSE, 1, 1, P1>(s, ibb, op, cfs, nb, r3, o);
         emit(I1{}, I1{}, NR1{}, t0b, nb, o, false);
     }
     return true;
 }
 
 // One CTA per work item.
-template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+template <typename T, int M2, int NH, int KIND, bool SPARSE>
 __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
     gs_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op, const __grid_constant__ BandMaps in,
                    const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
     extern __shared__ __align__(128) unsigned char band_smem[];
     __shared__ __align__(8) unsigned long long bar_store;
-    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+    __shared__ __align__(16) T cfs[KIND == OP_PLANE ? kCoefWords : 4];
     const int tid = threadIdx.x;
     const BandItem it = band_item(args, blockIdx.x);
     if (!band_stages<KIND>(it)) {
@@ -453,74 +496,8 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) band_issue<T, M2, JOUT>(args, in, out_maps, it, sbase, bar);
-    band_compute<T, M2, JOUT, NH, KIND, SPARSE>(args, op, it, reinterpret_cast<T *>(band_smem), cfs, bar, 0, r, xout);
-}
-
-// Persistent form: one CTA per SM walks the items blockIdx.x, + gridDim.x,
-// ..., with two staging buffers: the boxes of the item after next are issued
-// as soon as an item's compute has released its buffer, so the copy engine
-// streams while the SM computes.  Buffer b's mbarrier completes once per
-// staged item it receives, so its phase parity is its count of staged items.
-template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
-__global__ void __launch_bounds__(NH * M2, 1)
-    gs_band_persist_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op,
-                           const __grid_constant__ BandMaps in, const __grid_constant__ BandMaps out_maps,
-                           const T *__restrict__ r, T *__restrict__ xout) {
-    extern __shared__ __align__(128) unsigned char band_smem[];
-    __shared__ __align__(8) unsigned long long bar_store[2];
-    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
-    const int tid = threadIdx.x;
-    const int nitems = args.nbands * args.nplanes, G = gridDim.x;
-    constexpr unsigned BUFB = kBandWords<M2> * sizeof(T);
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(band_smem);
-    const unsigned bar0 = (unsigned)__cvta_generic_to_shared(&bar_store[0]);
-    if ((sbase & 127u) != 0) {
-        if (tid == 0) atomicExch(&g_band_err, 2);
-        return;
-    }
-    if (tid == 0) {
-        mbar_init(bar0, 1);
-        mbar_init(bar0 + 8, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    // the i-th item of this CTA uses buffer i & 1; items staged into each buffer so far
-    unsigned staged0 = 0, staged1 = 0;
-    if (tid == 0)
-        for (int i = 0; i < 2; i++) {
-            const int item = blockIdx.x + i * G;
-            if (item >= nitems) break;
-            const BandItem it = band_item(args, item);
-            if (band_stages<KIND>(it)) band_issue<T, M2, JOUT>(args, in, out_maps, it, sbase + i * BUFB, bar0 + 8 * i);
-        }
-    int i = 0;
-    for (int item = blockIdx.x; item < nitems; item += G, i++) {
-        const int buf = i & 1;
-        const BandItem it = band_item(args, item);
-        if (!band_stages<KIND>(it)) {
-            band_plate<T, M2, NH>(args.g, op.cop, it, args.c, r, xout);
-        } else {
-            T *s = reinterpret_cast<T *>(band_smem + buf * BUFB);
-            if (!band_compute<T, M2, JOUT, NH, KIND, SPARSE>(args, op, it, s, cfs, bar0 + 8 * buf,
-                                                             (buf ? staged1 : staged0) & 1, r, xout)) {
-                // the other buffer may still be receiving the next item's boxes
-                const int nxt = item + G;
-                if (tid == 0 && nxt < nitems && band_stages<KIND>(band_item(args, nxt)))
-                    mbar_wait(bar0 + 8 * (buf ^ 1), (buf ? staged0 : staged1) & 1, 200000000ull);
-                __syncthreads();
-                return;
-            }
-            if (buf) staged1++;
-            else staged0++;
-        }
-        __syncthreads();   // buffer buf (and cfs) free again
-        const int next = item + 2 * G;
-        if (tid == 0 && next < nitems) {
-            const BandItem nt = band_item(args, next);
-            if (band_stages<KIND>(nt)) band_issue<T, M2, JOUT>(args, in, out_maps, nt, sbase + buf * BUFB, bar0 + 8 * buf);
-        }
-    }
+    if (tid == 0) band_issue<T, M2>(args, in, out_maps, it, sbase, bar);
+    band_compute<T, M2, NH, KIND, SPARSE>(args, op, it, reinterpret_cast<T *>(band_smem), cfs, bar, 0, r, xout);
 }
 
 // ------------------------------------------------------------ residual
@@ -528,19 +505,67 @@ __global__ void __launch_bounds__(NH * M2, 1)
 // band's own rows (no chain between colours, so no halo row and no barrier
 // between them), in the arithmetic and order of residual_kernel
 // (const_row<T, ELASTIC, true> / plane_row_coef<T, SPARSE, true>).
-template <typename T, int M2, bool JOUT, int KIND, bool SPARSE, int A, int B, int NR>
+template <typename T, int M2, int KIND, bool SPARSE, int A, int B, int NR>
 __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const int (&ib)[3], const LevelOp<T> &op,
                                                 const T *cf, int t0, int nv, const Geom &g, int c, int K, int J0,
                                                 int I, const T *__restrict__ r, T *__restrict__ res) {
-    constexpr int rowstep = woff<M2, JOUT>(0, 0, 1, 0, 0);
+    constexpr int rowstep = woff<M2>(0, 0, 1, 0, 0);
     const size_t np = (size_t)g.npad;
+    if constexpr (KIND != OP_CONST) {
+        // plane k's coarse row, one block at a time: its 9 coefficients
+        // (16-byte shared loads) serve all of this thread's rows, each row
+        // taking its three values and its products in plane_row_coef's order
+        if (nv <= 0) return;
+        // rows past this thread's last repeat its last row (no branch inside
+        // the block loop; their results are not stored)
+        int roff[NR];
+        T acc[NR][3];
+#pragma unroll
+        for (int u = 0; u < NR; u++) {
+            const int t = t0 + min(u, nv - 1);
+            roff[u] = (t + 1) * rowstep;
+            const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
+            acc[u][0] = r[sl];
+            acc[u][1] = r[sl + np];
+            acc[u][2] = r[sl + 2 * np];
+        }
+        sfor<0, 27>([&](auto bi) {
+            constexpr int b = decltype(bi)::value;
+            constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+            constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+            constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+            asm volatile("" ::: "memory");
+            T cb[kCoefPad];
+            load_block_coef<T>(cf + kCoefPad * b, cb);
+#pragma unroll
+            for (int u = 0; u < NR; u++) {
+                const int base = ib[sI + 1] + roff[u] + sJ * rowstep;
+                T v[3];
+                v[0] = s[base + woff<M2>(1 + dz, 0, 0, ap + 2 * bp, 0)];
+                v[1] = s[base + woff<M2>(1 + dz, 1, 0, ap + 2 * bp, 0)];
+                v[2] = s[base + woff<M2>(1 + dz, 2, 0, ap + 2 * bp, 0)];
+#pragma unroll
+                for (int e = 0; e < 9; e++)
+                    if (!SPARSE || coarse_entry(b, e)) acc[u][e / 3] -= cb[e] * v[e % 3];
+            }
+        });
+#pragma unroll
+        for (int u = 0; u < NR; u++)
+            if (u < nv) {
+                const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t0 + u, I);
+                res[sl] = acc[u][0];
+                res[sl + np] = acc[u][1];
+                res[sl + 2 * np] = acc[u][2];
+            }
+        return;
+    }
 #pragma unroll 1
     for (int u = 0; u < NR; u++) {
         if (u >= nv) break;
         const int t = t0 + u, Jr = t + 1;
         const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
         T acc[3] = {r[sl], r[sl + np], r[sl + 2 * np]};
-        if constexpr (KIND == OP_CONST) {
+        {
             T v[27][3];
             sfor<0, 27>([&](auto bi) {
                 constexpr int b = decltype(bi)::value;
@@ -552,7 +577,7 @@ __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const i
                         constexpr int cc = decltype(ci)::value;
                         constexpr bool used =
                             b == 13 || elastic_entry(b, cc) || elastic_entry(b, 3 + cc) || elastic_entry(b, 6 + cc);
-                        if constexpr (used) v[b][cc] = s[ib[sI + 1] + woff<M2, JOUT>(1 + dz, cc, 0, ap + 2 * bp, 0) +
+                        if constexpr (used) v[b][cc] = s[ib[sI + 1] + woff<M2>(1 + dz, cc, 0, ap + 2 * bp, 0) +
                                                          (Jr + sJ) * rowstep];
                         else v[b][cc] = T(0);
                     });
@@ -573,24 +598,6 @@ __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const i
                     matvec_sub(op.cop.a[13], v[13], acc);
                 }
             }
-        } else {
-            // one block at a time (its three values, then its products in
-            // plane_row_coef's order): a whole row would not fit in registers
-            sfor<0, 27>([&](auto bi) {
-                constexpr int b = decltype(bi)::value;
-                constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
-                constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
-                constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
-                asm volatile("" ::: "memory");
-                const int base = ib[sI + 1] + (Jr + sJ) * rowstep;
-                T v[3];
-                v[0] = s[base + woff<M2, JOUT>(1 + dz, 0, 0, ap + 2 * bp, 0)];
-                v[1] = s[base + woff<M2, JOUT>(1 + dz, 1, 0, ap + 2 * bp, 0)];
-                v[2] = s[base + woff<M2, JOUT>(1 + dz, 2, 0, ap + 2 * bp, 0)];
-#pragma unroll
-                for (int e = 0; e < 9; e++)
-                    if (!SPARSE || coarse_entry(b, e)) acc[e / 3] -= cf[9 * b + e] * v[e % 3];
-            });
         }
         res[sl] = acc[0];
         res[sl + np] = acc[1];
@@ -598,13 +605,13 @@ __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const i
     }
 }
 
-template <typename T, int M2, bool JOUT, int NH, int KIND, bool SPARSE>
+template <typename T, int M2, int NH, int KIND, bool SPARSE>
 __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
     residual_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op,
                          const __grid_constant__ BandMaps xm, const T *__restrict__ r, T *__restrict__ res) {
     extern __shared__ __align__(128) unsigned char band_smem[];
     __shared__ __align__(8) unsigned long long bar_store;
-    __shared__ T cfs[KIND == OP_PLANE ? 252 : 1];
+    __shared__ __align__(16) T cfs[KIND == OP_PLANE ? kCoefWords : 4];
     const Geom &g = args.g;
     const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
     const int band = blockIdx.x % args.nbands, k = blockIdx.x / args.nbands;
@@ -641,13 +648,11 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
         const unsigned plane_bytes = (unsigned)(kBandWords<M2> / 3 * sizeof(T));
         mbar_expect_tx(bar, plane_bytes * (1u + has_lo + has_hi));
         const int klo = k == 0 ? g.o - 1 : k - 1, khi = k == g.o - 1 ? 0 : k + 1;
-        if (has_lo) stage_plane<T, M2, JOUT>(xm, g, klo, J0, 0, sbase, bar);
-        stage_plane<T, M2, JOUT>(xm, g, k, J0, 1, sbase, bar);
-        if (has_hi) stage_plane<T, M2, JOUT>(xm, g, khi, J0, 2, sbase, bar);
+        if (has_lo) stage_plane<T, M2>(xm, g, klo, J0, 0, sbase, bar);
+        stage_plane<T, M2>(xm, g, k, J0, 1, sbase, bar);
+        if (has_hi) stage_plane<T, M2>(xm, g, khi, J0, 2, sbase, bar);
     }
-    if (KIND == OP_PLANE)
-        for (int e = tid; e < 252; e += NH * M2)
-            cfs[e] = e < 243 ? op.pop.coef[e * op.pop.O + k] : op.pop.dinv[(e - 243) * op.pop.O + k];
+    if (KIND == OP_PLANE) stage_coef<T>(op.pop, k, cfs, tid, NH * M2);
     const bool ok = mbar_wait(bar, 0, 200000000ull);
     if (!__syncthreads_and(ok)) {
         if (tid == 0) {
@@ -669,10 +674,18 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
     constexpr int P = kPer<kOwnSub, NH>;
     const int t0 = hh * P, nv = min(P, kOwnSub - t0);
     const int ib[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
-    band_res_colour<T, M2, JOUT, KIND, SPARSE, 0, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
-    band_res_colour<T, M2, JOUT, KIND, SPARSE, 1, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
-    band_res_colour<T, M2, JOUT, KIND, SPARSE, 0, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
-    band_res_colour<T, M2, JOUT, KIND, SPARSE, 1, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+    // the four colours as the branches of a loop that is not unrolled: the
+    // colours share no barrier, and in one straight run the instruction
+    // scheduler would start every colour's shared loads at once
+#pragma unroll 1
+    for (int q = 0; q < 4; q++) {
+        switch (q) {
+            case 0: band_res_colour<T, M2, KIND, SPARSE, 0, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res); break;
+            case 1: band_res_colour<T, M2, KIND, SPARSE, 1, 0, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res); break;
+            case 2: band_res_colour<T, M2, KIND, SPARSE, 0, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res); break;
+            default: band_res_colour<T, M2, KIND, SPARSE, 1, 1, P>(s, ib, op, cfs, t0, nv, g, c, K, J0, I, r, res);
+        }
+    }
 }
 
 // ------------------------------------------------------------------ host
@@ -698,59 +711,29 @@ EncodeTiled encoder() {
 }
 
 // The tensor maps of one colour-blocked field of level g: a 5-d view with
-// column I innermost, then (JOUT) colour ab, sub-row J, plane K, component x
-// plane parity -- or (not JOUT) J, K, ab -- and boxes of the whole row of M2
-// columns, 4 colours (JOUT) or one, and 6, 5 or 1 sub-rows.
-template <typename T, bool JOUT>
+// column I innermost, then colour ab, sub-row J, plane K, component x plane
+// parity, and boxes of the whole row of M2 columns, 4 colours and 6, 5 or 1
+// sub-rows.  False if the driver does not accept them (the caller then runs
+// the colour launches).
+template <typename T>
 bool make_band_maps(const Geom &g, const T *field, BandMaps &mp) {
     EncodeTiled enc = encoder();
     if (!enc) return false;
     const cuuint64_t e = sizeof(T);
     const cuuint64_t M2 = g.M2, N2 = g.N2, O2 = g.O2, S = g.S;
-    cuuint64_t dims[5], strides[4];
-    if (JOUT) {
-        const cuuint64_t d[5] = {M2, 4, N2, O2, 6}, st[4] = {S * e, M2 * e, M2 * N2 * e, 4 * S * e};
-        std::memcpy(dims, d, sizeof d);
-        std::memcpy(strides, st, sizeof st);
-    } else {
-        const cuuint64_t d[5] = {M2, N2, O2, 4, 6}, st[4] = {M2 * e, M2 * N2 * e, S * e, 4 * S * e};
-        std::memcpy(dims, d, sizeof d);
-        std::memcpy(strides, st, sizeof st);
-    }
+    const cuuint64_t dims[5] = {M2, 4, N2, O2, 6}, strides[4] = {S * e, M2 * e, M2 * N2 * e, 4 * S * e};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
     CUtensorMap *maps[3] = {&mp.rows6, &mp.rows5, &mp.rows1};
     const cuuint32_t rows[3] = {kStageRows, kStageRows - 1, 1};
     for (int i = 0; i < 3; i++) {
-        cuuint32_t box[5];
-        if (JOUT) {
-            const cuuint32_t b[5] = {(cuuint32_t)M2, 4, rows[i], 1, 1};
-            std::memcpy(box, b, sizeof b);
-        } else {
-            const cuuint32_t b[5] = {(cuuint32_t)M2, rows[i], 1, 1, 1};
-            std::memcpy(box, b, sizeof b);
-        }
+        const cuuint32_t box[5] = {(cuuint32_t)M2, 4, rows[i], 1, 1};
         if (enc(maps[i], dt, 5, const_cast<T *>(field), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return false;
     }
     return true;
-}
-
-// Layout of the tensor maps the driver accepts: 1 the colour-inner view (one
-// box per plane and component), 0 the monotonic view (one box per colour),
-// -1 neither (the colour launches run instead).  Decided once per process.
-template <typename T>
-int band_layout(const Geom &g, const T *field) {
-    static int layout = -2;
-    if (layout == -2) {
-        BandMaps mp;
-        if (make_band_maps<T, true>(g, field, mp)) layout = 1;
-        else if (make_band_maps<T, false>(g, field, mp)) layout = 0;
-        else layout = -1;
-    }
-    return layout;
 }
 
 bool first_band_use(unsigned long long &devices) {
@@ -762,69 +745,24 @@ bool first_band_use(unsigned long long &devices) {
     return true;
 }
 
-// Threads per column of the band kernel: two on wide FP32 levels (twice the
-// warps for the same shared memory), four on narrow ones (a level of 8-32
-// sub-grid columns has few nodes per row), one or two in FP64 (shared
-// memory and registers)
+// Threads per column of the residual kernel: two (each thread two of the
+// band's four sub-rows; with one row, or four, the plane-invariant row's
+// products take more registers than a thread has).
 template <typename T, int M2>
-constexpr int kBandNH = sizeof(T) == 4 ? (M2 >= 64 ? 2 : 4) : (M2 >= 64 ? 1 : 2);
+constexpr int kResNH = 2;
 
-// The persistent double-buffered form (STZ_MG_BAND_PERSIST=1) or one CTA per item.
-bool band_persist() {
-    const char *e = std::getenv("STZ_MG_BAND_PERSIST");
-    return e && std::atoi(e) != 0;
-}
-
-template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
-bool launch_band_persist(const LevelOp<T> &op, const Geom &g, const T *r, const BandMaps &min_,
-                         const BandMaps &mout, T *xout, cudaStream_t st) {
-    constexpr int NH = sizeof(T) == 4 ? 4 : 1;
-    auto kern = gs_band_persist_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
-    const int smem = 2 * kBandWords<M2> * (int)sizeof(T);
-    static unsigned long long attr_devices = 0;
-    static int per_sm = 0, sms = 0;
-    if (first_band_use(attr_devices)) {
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        per_sm = 0;
-        // two staging buffers must fit one CTA's shared memory
-        if (smem <= optin && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NH * M2, smem) != cudaSuccess)
-            per_sm = 0;
-        cudaGetLastError();
-    }
-    if (per_sm < 1 || sms < 1) return false;
-    BandArgs a;
-    a.g = g;
-    a.nbands = g.n / kBandRows;
-    for (int c = 0; c < 2; c++) {
-        const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
-        if (planes <= 0) continue;
-        a.c = c;
-        a.nplanes = planes;
-        a.rev = c;
-        const int grid = std::min(a.nbands * planes, per_sm * sms);
-        kern<<<grid, NH * M2, smem, st>>>(a, op, min_, mout, r, xout);
-    }
-    return true;
-}
-
-template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
-bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+template <typename T, int M2, int NH, int KIND, bool SPARSE>
+bool launch_band_kn(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     BandMaps min_, mout;
-    if (!make_band_maps<T, JOUT>(g, xin, min_) || !make_band_maps<T, JOUT>(g, xout, mout)) return false;
-    // the persistent form where its two buffers fit, else one CTA per item
-    if (band_persist() && launch_band_persist<T, M2, JOUT, KIND, SPARSE>(op, g, r, min_, mout, xout, st)) return true;
-    constexpr int NH = kBandNH<T, M2>;
-    auto kern = gs_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
+    if (!make_band_maps<T>(g, xin, min_) || !make_band_maps<T>(g, xout, mout)) return false;
+    auto kern = gs_band_kernel<T, M2, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);
     static unsigned long long attr_devices = 0;
     if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     BandArgs a;
     a.g = g;
     a.nbands = g.n / kBandRows;
+    a.xz = nullptr;
     for (int c = 0; c < 2; c++) {
         const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
         if (planes <= 0) continue;
@@ -839,23 +777,34 @@ bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin
     return true;
 }
 
-template <typename T, bool JOUT, int KIND, bool SPARSE>
+// Threads per column of the sweep: in FP32 two on wide levels (64 or 128
+// sub-grid columns; four, with twice the warps, measured no faster: 350 vs
+// 347 us for two fine sweeps, 131 vs 126 us on level 1, where a thread's
+// three rows share each coefficient load) and four on narrow ones (few nodes
+// per row); one or two in FP64 (shared memory and registers).
+template <typename T, int M2, int KIND, bool SPARSE>
+bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
+    constexpr int NH = sizeof(T) == 8 ? (M2 >= 64 ? 1 : 2) : (M2 >= 64 ? 2 : 4);
+    return launch_band_kn<T, M2, NH, KIND, SPARSE>(op, g, r, xin, xout, st);
+}
+
+template <typename T, int KIND, bool SPARSE>
 bool launch_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
     switch (g.M2) {
-        case 8: return launch_band_k<T, 8, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
-        case 16: return launch_band_k<T, 16, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
-        case 32: return launch_band_k<T, 32, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
-        case 64: return launch_band_k<T, 64, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
-        case 128: return launch_band_k<T, 128, JOUT, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 8: return launch_band_k<T, 8, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 16: return launch_band_k<T, 16, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 32: return launch_band_k<T, 32, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 64: return launch_band_k<T, 64, KIND, SPARSE>(op, g, r, xin, xout, st);
+        case 128: return launch_band_k<T, 128, KIND, SPARSE>(op, g, r, xin, xout, st);
         default: return false;
     }
 }
 
-template <typename T, bool JOUT>
+template <typename T>
 bool launch_band_op(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
-    if (op.kind == OP_CONST) return launch_band_m<T, JOUT, OP_CONST, false>(op, g, r, xin, xout, st);
-    if (op.pop.sparse) return launch_band_m<T, JOUT, OP_PLANE, true>(op, g, r, xin, xout, st);
-    return launch_band_m<T, JOUT, OP_PLANE, false>(op, g, r, xin, xout, st);
+    if (op.kind == OP_CONST) return launch_band_m<T, OP_CONST, false>(op, g, r, xin, xout, st);
+    if (op.pop.sparse) return launch_band_m<T, OP_PLANE, true>(op, g, r, xin, xout, st);
+    return launch_band_m<T, OP_PLANE, false>(op, g, r, xin, xout, st);
 }
 
 }  // namespace
@@ -882,20 +831,17 @@ bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
 // caller then sweeps with the colour launches).
 template <typename T>
 bool launch_gs_sweep_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
-    const int layout = band_layout<T>(g, xin);
-    if (layout == 1) return launch_band_op<T, true>(op, g, r, xin, xout, st);
-    if (layout == 0) return launch_band_op<T, false>(op, g, r, xin, xout, st);
-    return false;
+    return launch_band_op<T>(op, g, r, xin, xout, st);
 }
 
 namespace {
 
-template <typename T, int M2, bool JOUT, int KIND, bool SPARSE>
+template <typename T, int M2, int KIND, bool SPARSE>
 bool launch_res_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
     BandMaps xm;
-    if (!make_band_maps<T, JOUT>(g, x, xm)) return false;
-    constexpr int NH = kBandNH<T, M2>;
-    auto kern = residual_band_kernel<T, M2, JOUT, NH, KIND, SPARSE>;
+    if (!make_band_maps<T>(g, x, xm)) return false;
+    constexpr int NH = kResNH<T, M2>;
+    auto kern = residual_band_kernel<T, M2, NH, KIND, SPARSE>;
     const int smem = kBandWords<M2> * (int)sizeof(T);
     static unsigned long long attr_devices = 0;
     if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -910,36 +856,40 @@ bool launch_res_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T 
     return true;
 }
 
-template <typename T, bool JOUT, int KIND, bool SPARSE>
+template <typename T, int KIND, bool SPARSE>
 bool launch_res_band_m(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
     switch (g.M2) {
-        case 8: return launch_res_band_k<T, 8, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
-        case 16: return launch_res_band_k<T, 16, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
-        case 32: return launch_res_band_k<T, 32, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
-        case 64: return launch_res_band_k<T, 64, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
-        case 128: return launch_res_band_k<T, 128, JOUT, KIND, SPARSE>(op, g, r, x, res, st);
+        case 8: return launch_res_band_k<T, 8, KIND, SPARSE>(op, g, r, x, res, st);
+        case 16: return launch_res_band_k<T, 16, KIND, SPARSE>(op, g, r, x, res, st);
+        case 32: return launch_res_band_k<T, 32, KIND, SPARSE>(op, g, r, x, res, st);
+        case 64: return launch_res_band_k<T, 64, KIND, SPARSE>(op, g, r, x, res, st);
+        case 128: return launch_res_band_k<T, 128, KIND, SPARSE>(op, g, r, x, res, st);
         default: return false;
     }
 }
 
-template <typename T, bool JOUT>
+template <typename T>
 bool launch_res_band_op(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
-    if (op.kind == OP_CONST) return launch_res_band_m<T, JOUT, OP_CONST, false>(op, g, r, x, res, st);
-    if (op.pop.sparse) return launch_res_band_m<T, JOUT, OP_PLANE, true>(op, g, r, x, res, st);
-    return launch_res_band_m<T, JOUT, OP_PLANE, false>(op, g, r, x, res, st);
+    if (op.kind == OP_CONST) return launch_res_band_m<T, OP_CONST, false>(op, g, r, x, res, st);
+    if (op.pop.sparse) return launch_res_band_m<T, OP_PLANE, true>(op, g, r, x, res, st);
+    return launch_res_band_m<T, OP_PLANE, false>(op, g, r, x, res, st);
 }
 
 }  // namespace
 
-// res = r - A x by the band kernel where the band sweep applies; false (the
-// caller falls back) where it does not or the tensor maps cannot be made.
+// res = r - A x by the band kernel on the plane-invariant levels the band
+// sweep serves; false (the caller falls back) elsewhere or when the tensor
+// maps cannot be made.  On the shared-stencil fine level the marching tiled
+// residual is faster (each plane staged once instead of three times: 169 vs
+// 232 us at 256x256x257), so the band residual runs there only with
+// STZ_MG_BAND_RES=1; STZ_MG_BAND_RES=0 turns it off everywhere.
 template <typename T>
 bool launch_residual_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st) {
     if (!gs_band_applies(op, g)) return false;
-    const int layout = band_layout<T>(g, x);
-    if (layout == 1) return launch_res_band_op<T, true>(op, g, r, x, res, st);
-    if (layout == 0) return launch_res_band_op<T, false>(op, g, r, x, res, st);
-    return false;
+    int mode = -1;
+    if (const char *e = std::getenv("STZ_MG_BAND_RES")) mode = std::atoi(e) != 0;
+    if (mode == 0 || (mode < 0 && op.kind != OP_PLANE)) return false;
+    return launch_res_band_op<T>(op, g, r, x, res, st);
 }
 template bool launch_residual_band<float>(const LevelOp<float> &, const Geom &, const float *, const float *, float *,
                                           cudaStream_t);
@@ -949,7 +899,8 @@ template bool launch_residual_band<double>(const LevelOp<double> &, const Geom &
 // Whether the tensor maps of the band sweep can be made for this level.
 template <typename T>
 bool gs_band_ready(const Geom &g, const T *field) {
-    return band_layout<T>(g, field) >= 0;
+    BandMaps mp;
+    return make_band_maps<T>(g, field, mp);
 }
 template bool gs_band_ready<float>(const Geom &, const float *);
 template bool gs_band_ready<double>(const Geom &, const double *);

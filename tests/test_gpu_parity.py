@@ -331,22 +331,19 @@ BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64
                     ((64, 64, 33), (True, True, False), "const", 1, 2), ((64, 32, 16), (True, True, True), "trans", 1, 2)]
 
 
-@pytest.mark.parametrize("persist", ["0", "1"])
 @pytest.mark.parametrize("dims,per,kind,level,sweeps", BAND_LEVEL_CASES)
-def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, persist, monkeypatch):
+def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, monkeypatch):
     """The band sweep (full-width bands of 8 rows, planes staged by TMA boxes,
     split at the periodic wrap in y) gives bit for bit the result of the eight
     colour launches: FP64 level sweeps of the elasticity stencil on the fine
     level and of the plane-invariant coarse operators (sparse elastic and
     full from a non-symmetric stencil) on level 1, Dirichlet and periodic z,
-    32, 64 and 128 sub-grid columns, two bands (both at the wrap) and many,
-    even and odd sweep counts; with a CTA per band and plane, and with the
-    persistent form (a CTA per SM, two staging buffers, STZ_MG_BAND_PERSIST=1)."""
+    8 to 128 sub-grid columns, two bands (both at the wrap) and many, even
+    and odd sweep counts."""
     import stzpp_gb300 as sg
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per)
     st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(2, h[0])
-    monkeypatch.setenv("STZ_MG_BAND_PERSIST", persist)
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
@@ -363,10 +360,9 @@ def test_band_sweep_is_the_colour_sweep(dims, per, kind, level, sweeps, persist,
     assert np.array_equal(out["0"], out["1"])
 
 
-@pytest.mark.parametrize("persist", ["0", "1"])
 @pytest.mark.parametrize("dims,per", [((128, 128, 33), (True, True, False)), ((256, 256, 17), (True, True, False)),
                                       ((128, 64, 24), (True, True, False))])
-def test_band_sweep_mixed_solve_bitwise(dims, per, persist, monkeypatch):
+def test_band_sweep_mixed_solve_bitwise(dims, per, monkeypatch):
     """The FP32 V-cycles of the mixed solve with the band sweep on the fine
     level (the default) and with the colour launches give the same cycle
     count and the same solution bit for bit (an even plane count puts the
@@ -375,7 +371,6 @@ def test_band_sweep_mixed_solve_bitwise(dims, per, persist, monkeypatch):
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per, h=1.0 / m)
     b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
-    monkeypatch.setenv("STZ_MG_BAND_PERSIST", persist)
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
@@ -442,18 +437,22 @@ def test_fourier_bottom_inverse_is_the_dense_inverse(dims, kind, precision, monk
     assert np.linalg.norm(x1 - x0) <= 1e-11 * np.linalg.norm(x0)
 
 
+@pytest.mark.parametrize("bandres", ["default", "1"])
 @pytest.mark.parametrize("dims,per,kind", [((128, 128, 33), (True, True, False), "const"),
                                           ((128, 64, 24), (True, True, False), "trans"),
                                           ((64, 64, 32), (True, True, False), "const")])
-def test_band_kernels_fp64_solve_bitwise(dims, per, kind, monkeypatch):
+def test_band_kernels_fp64_solve_bitwise(dims, per, kind, bandres, monkeypatch):
     """FP64 solves with the band kernels forced (STZ_MG_BAND=1: the band sweep
-    and the band residual on every level they serve) and without: the same
-    cycle count and the same solution bit for bit."""
+    on every level it serves and the band residual on the plane-invariant
+    ones, or with STZ_MG_BAND_RES=1 on the fine level too) and without: the
+    same cycle count and the same solution bit for bit."""
     import stzpp_gb300 as sg
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per, h=1.0 / m)
     b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
     st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(1, h[0])
+    if bandres != "default":
+        monkeypatch.setenv("STZ_MG_BAND_RES", bandres)
     out = {}
     for band in ("0", "1"):
         monkeypatch.setenv("STZ_MG_BAND", band)
@@ -462,5 +461,39 @@ def test_band_kernels_fp64_solve_bitwise(dims, per, kind, monkeypatch):
             mg.setup_fields(r=b)
             cyc, rel = mg.solve(1e-10, 6, check=False)
             out[band] = (cyc, rel, mg.get_x())
+    assert out["0"][:2] == out["1"][:2]
+    assert np.array_equal(out["0"][2], out["1"][2])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("dims,per,kind", [((128, 128, 33), (True, True, False), "const"),
+                                          ((128, 64, 32), (True, True, False), "const"),
+                                          ((64, 64, 16), (True, True, True), "const"),
+                                          ((128, 64, 25), (True, True, False), "trans"),
+                                          ((256, 256, 17), (True, True, False), "const")])
+def test_fused_residual_restriction_is_the_two_kernels(dims, per, kind, precision, monkeypatch):
+    """The descent's residual and restriction in one pass (the residual never
+    written) against the residual kernel followed by the restriction kernel:
+    the same cycle count and the same solution bit for bit, through whole
+    solves -- FP32 V-cycles of the mixed solver and FP64 ones (STZ_MG_TILE=1,
+    the tiled kernels in FP64 too), the elastic and a full non-symmetric
+    shared stencil, an odd and an even Dirichlet z (the even one puts the
+    last fine plane under the last coarse plane alone) and a periodic z."""
+    import stzpp_gb300 as sg
+    m, n, o = dims
+    h = P.grid_spacing(m, n, o, per, h=1.0 / m)
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, *h)
+    st, fix = sg.elastic_stencil(1.0, 2.0, *h) if kind == "const" else trans_stencil(1, h[0])
+    if precision == "fp64":
+        monkeypatch.setenv("STZ_MG_TILE", "1")
+    out = {}
+    for fused in ("0", "1"):
+        monkeypatch.setenv("STZ_MG_FUSED_RESTRICT", fused)
+        with sg.Multigrid(dims, per, precision=precision, sweep_growth=False, v_down=2, v_up=2) as mg:
+            mg.setup_matrices(stencil=st, fix=fix)
+            mg.setup_fields(r=b)
+            cyc, rel = mg.solve(1e-10, 6, check=False)
+            out[fused] = (cyc, rel, mg.get_x())
+    assert np.isfinite(out["0"][1]) and out["0"][1] < 1e-2
     assert out["0"][:2] == out["1"][:2]
     assert np.array_equal(out["0"][2], out["1"][2])
