@@ -863,8 +863,10 @@ void enqueue_vcycle(stz_mg_handle h, Hier<T> H) {
         const Geom &g = h->geo[i];
         launch_gs_sweeps<T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, h->d.v_down + (h->d.sweep_growth ? i : 0),
                             h->st);
-        launch_residual<T, T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, nullptr, nullptr, h->st);
-        launch_restriction<T>(g, h->geo[i + 1], H.L[i].res, H.L[i + 1].r, h->st);
+        if (!launch_residual_restrict<T>(H.op[i], g, h->geo[i + 1], H.L[i].r, H.L[i].x, H.L[i + 1].r, h->st)) {
+            launch_residual<T, T>(H.op[i], g, H.L[i].r, H.L[i].x, H.L[i].res, nullptr, nullptr, h->st);
+            launch_restriction<T>(g, h->geo[i + 1], H.L[i].res, H.L[i + 1].r, h->st);
+        }
         CK(cudaMemsetAsync(H.L[i + 1].x, 0, 3 * (size_t)h->geo[i + 1].npad * sizeof(T), h->st));
     }
     TailDesc<T> td{};

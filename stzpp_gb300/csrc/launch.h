@@ -47,6 +47,12 @@ bool gs_band_ready(const Geom &g, const T *field);
 // sweep applies (no norm); false where it does not
 template <typename T>
 bool launch_residual_band(const LevelOp<T> &op, const Geom &g, const T *r, const T *x, T *res, cudaStream_t st);
+// tile.cu: rc = R (r - A x) in one pass on the levels the tiled residual
+// serves with a shared stencil (the fine level's residual never written;
+// opt-in, STZ_MG_FUSED_RESTRICT=1); false where it does not apply
+template <typename T>
+bool launch_residual_restrict(const LevelOp<T> &op, const Geom &g, const Geom &gc, const T *r, const T *x, T *rc,
+                              cudaStream_t st);
 // How launch_gs_sweeps smooths a level: 0 eight colour launches per sweep,
 // 1 the tiled two-buffer sweep, 2 the band sweep, 3 the plane-phase kernels
 // (two launches per sweep each but the first)

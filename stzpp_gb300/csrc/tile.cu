@@ -30,6 +30,7 @@
 
 #include "launch.h"
 #include "ops.cuh"
+#include "transfer.cuh"
 
 namespace stzmg {
 
@@ -586,6 +587,272 @@ void launch_res_tile_k(const LevelOp<T> &op, const Geom &g, const T *r, const T 
             <<<grid, kTileThreads, smem, st>>>(g, op, r, x, res, partial, zlen);
 }
 
+// ------------------------------------------- residual fused with restriction
+// The descent of the V-cycle computes res = r - A x on a level and restricts
+// it at once (multigrid.cc:253-297: region::compute_rats residual, then
+// region::restrict, region.cc:2129-2186); res itself is read by nothing else.
+// The fused kernel never writes it: each CTA takes a 32 x 32 tile of the fine
+// level (16 x 16 coarse columns) and marches up z through a chunk of coarse
+// planes, computing the residual of every fine plane on the tile widened by
+// one node towards lower x and y (the children 2I - 1 of its first coarse
+// row and column) into shared memory and adding it, with the restriction's
+// weights, to the coarse nodes it belongs to.  A coarse node collects its
+// fine planes 2K - 1, 2K, 2K + 1 in that order, and within a plane the rows
+// and nodes in the restriction kernel's order, so its sum is the restriction
+// kernel's bit for bit; the residual values are residual_tile_kernel's.
+//
+// Staged x rows: tile rows -2 .. 32 (buffer rows 0 .. 34), in the ring slots
+// of the marching residual; the residual plane is [component][y + 1][x + 1]
+// for tile nodes x, y = -1 .. 31, rows kRP words apart.
+constexpr int kRR0 = kHalo - 2, kRowsRR = kTY + 3;
+constexpr int kRRSlot = 3 * kRowsRR * RS;
+constexpr int kRP = kTX + 2, kRPlane = (kTY + 1) * kRP;
+constexpr int kRRSmemWords = kRing * kRRSlot + 3 * kRPlane;
+
+// res = r - A x at one staged node of x-parity A (residual_tile_kernel's
+// arithmetic: the shared stencil with its centre block, or r - fix x on a
+// Dirichlet plate).
+template <typename T, bool ELASTIC, int A>
+__device__ __forceinline__ void rr_node(const ConstOp<T> &op, const unsigned (&cz)[3], bool zin, T *acc) {
+    if (zin) {
+        tile_const_row<T, ELASTIC, true, A, kRowsRR>(op, cz, acc);
+    } else {
+        T v[3];
+        lds<nb_off<A, kRowsRR>(13, 0)>(cz[1], v[0]);
+        lds<nb_off<A, kRowsRR>(13, 1)>(cz[1], v[1]);
+        lds<nb_off<A, kRowsRR>(13, 2)>(cz[1], v[2]);
+        matvec_sub(op.fix, v, acc);
+    }
+}
+
+// One residual node (tile coordinates ii, jj of the widened tile) of plane k
+// into the residual plane; r of the node in rv.
+template <typename T, bool ELASTIC>
+__device__ __forceinline__ void rr_store(const ConstOp<T> &op, unsigned s0, unsigned s1, unsigned s2, int ii, int jj,
+                                         bool zin, const T (&rv)[3], T *resp) {
+    const unsigned cw = (unsigned)(corner_word<kRR0>(ii, jj) * (int)sizeof(T));
+    const unsigned cz[3] = {s0 + cw, s1 + cw, s2 + cw};
+    T acc[3] = {rv[0], rv[1], rv[2]};
+    if (ii & 1) rr_node<T, ELASTIC, 1>(op, cz, zin, acc);
+    else rr_node<T, ELASTIC, 0>(op, cz, zin, acc);
+    const int w = (jj - kHalo + 1) * kRP + (ii - kHalo + 1);
+    resp[w] = acc[0];
+    resp[kRPlane + w] = acc[1];
+    resp[2 * kRPlane + w] = acc[2];
+}
+
+// Add fine plane kk's residual to the coarse nodes of this thread it is a
+// child of along z: with weight w0 to acc0 (if w0 != 0) and w1 to acc1 (if
+// w1 != 0; an odd plane closes one coarse plane and opens the next).  The 9
+// children in the plane go in the restriction's order (rows, then nodes),
+// weights 1/8 (1/2, 1, 1/2) in x and y times the z weight; each row's three
+// values per component come in one 8- or 16-byte and one scalar shared load
+// and serve both sums.
+template <typename T>
+__device__ __forceinline__ void rr_add(const T *resp, int ci, int cj, T w0, T *acc0, T w1, T *acc1) {
+    using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+    const bool d0 = w0 != T(0), d1 = w1 != T(0);
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        T v[3][3];
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            const T *row = resp + cc * kRPlane + (2 * cj + b) * kRP + 2 * ci;
+            const V2 p = *reinterpret_cast<const V2 *>(row);
+            v[cc][0] = p.x;
+            v[cc][1] = p.y;
+            v[cc][2] = row[2];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T wxy = T(0.125) * (c == 1 ? T(1) : T(0.5)) * (b == 1 ? T(1) : T(0.5));
+            if (d0) {
+                const T w = wxy * w0;
+                acc0[0] += w * v[0][c];
+                acc0[1] += w * v[1][c];
+                acc0[2] += w * v[2][c];
+            }
+            if (d1) {
+                const T w = wxy * w1;
+                acc1[0] += w * v[0][c];
+                acc1[1] += w * v[1][c];
+                acc1[2] += w * v[2][c];
+            }
+        }
+    }
+}
+
+// Threads of the fused kernel: the marching residual's 256 (four nodes of the
+// tile each, and one coarse node each) and a ninth warp for the 65 nodes of
+// the widened row and column (three each), so that no thread has more than
+// four residual nodes per plane.
+constexpr int kRRThreads = kTileThreads + 32;
+constexpr int kRRExtra = kTY + 1 + kTX;   // nodes of the column x = -1 and the row y = -1
+constexpr int kRRPer = (kRRExtra + 31) / 32;
+
+// rc = R (r - A x) for the coarse planes K0 .. K0 + zc - 1 of one tile; the
+// level is periodic in x and y, its operator the shared stencil.
+template <typename T, bool ELASTIC>
+__global__ void __launch_bounds__(kRRThreads, kMarchMinBlocks<T>)
+    res_restrict_kernel(Geom g, Geom gc, const __grid_constant__ LevelOp<T> op, const T *__restrict__ r,
+                        const T *__restrict__ x, T *__restrict__ rc, int zc) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    T *resp = reinterpret_cast<T *>(smem_raw) + kRing * kRRSlot;
+    const int ntx = g.m / kTX;
+    const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+    const int K0 = (int)blockIdx.y * zc, K1 = min(gc.o, K0 + zc);
+    const int i0 = tx * kTX - kHalo, j0 = ty * kTY - kHalo;
+    const size_t np = (size_t)g.npad;
+    // fine planes 2 K0 - 1 .. 2 K1 - 1, unwrapped (outside a Dirichlet z: none)
+    const int kf0 = 2 * K0 - 1, kf1 = 2 * K1 - 1;
+    auto exists = [&](int kk) { return g.zp || (kk >= 0 && kk < g.o); };
+    auto wrapk = [&](int kk) { return kk < 0 ? kk + g.o : (kk >= g.o ? kk - g.o : kk); };
+    auto xslot = [&](int kk) { return sbase + (unsigned)(((kk + 2 * kRing) % kRing) * kRRSlot * (int)sizeof(T)); };
+
+    // cp.async groups: {x of kf0-1, kf0, kf0+1}, {x of kf0+2}, then one per plane kk: {x of kk+3}
+    Stager<T, kRR0, kRowsRR, kRR0, kRowsRR, kRRThreads> st;
+    st.init(g, (i0 >> 1) - kHOff, j0);
+    for (int kk = kf0 - 1; kk <= kf0 + 1; kk++)
+        if (kk <= kf1 + 1 && exists(kk)) st.stage(g, x, wrapk(kk), xslot(kk));
+    copy_commit();
+    if (kf0 + 2 <= kf1 + 1 && exists(kf0 + 2)) st.stage(g, x, wrapk(kf0 + 2), xslot(kf0 + 2));
+    copy_commit();
+
+    // residual nodes of this thread: threads 0 .. 255 four of the tile
+    // (residual_tile_kernel's mapping), the ninth warp up to three of the
+    // widened column x = -1 (e = 0 .. 32: y = e - 1) and row y = -1
+    // (e = 33 .. 64: x = e - 33), e = lane + 32 u
+    const int te = (int)threadIdx.x;
+    const bool main = te < kTileThreads;
+    const int xs = te & 15, h = (te >> 4) & 1, a = (te >> 5) & 1;
+    const int b = (te >> 6) & 1, pr0 = h + 2 * ((te >> 7) & 1);
+    const int ii = kHalo + a + 2 * xs, i = wrapn(i0 + ii, g.m);
+    const int lane = te & 31;
+    auto enode = [&](int u, int &eii, int &ejj) {
+        const int e = lane + 32 * u;
+        eii = e <= kTY ? kHalo - 1 : kHalo + e - (kTY + 1);
+        ejj = e <= kTY ? kHalo - 1 + e : kHalo - 1;
+        return e < kRRExtra;
+    };
+    // this thread's coarse node (threads 0 .. 255)
+    const int ci = te & 15, cj = (te >> 4) & 15;
+    const int Ic = tx * (kTX / 2) + ci, Jc = ty * (kTY / 2) + cj;
+    // r of this thread's nodes of plane kk (unwrapped), loaded a plane ahead
+    constexpr int NV = 4 > kRRPer ? 4 : kRRPer;
+    auto load_r = [&](int kk, T (&rv)[NV][3]) {
+        if (!exists(kk)) return;
+        const int k = wrapk(kk);
+        if (main) {
+#pragma unroll
+            for (int it = 0; it < 4; it++) {
+                const int j = wrapn(j0 + kHalo + b + 2 * (pr0 + 4 * it), g.n);
+                const int s = (a + 2 * b + 4 * (k & 1)) * g.S + ((k >> 1) * g.N2 + (j >> 1)) * g.M2 + (i >> 1);
+                rv[it][0] = __ldcs(r + s);
+                rv[it][1] = __ldcs(r + s + np);
+                rv[it][2] = __ldcs(r + s + 2 * np);
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < kRRPer; u++) {
+                int eii, ejj;
+                if (enode(u, eii, ejj)) {
+                    const int ei = wrapn(i0 + eii, g.m), ej = wrapn(j0 + ejj, g.n);
+                    const int s = ((ei & 1) + 2 * (ej & 1) + 4 * (k & 1)) * g.S +
+                                  ((k >> 1) * g.N2 + (ej >> 1)) * g.M2 + (ei >> 1);
+                    rv[u][0] = r[s];
+                    rv[u][1] = r[s + np];
+                    rv[u][2] = r[s + 2 * np];
+                }
+            }
+        }
+    };
+    T acc[3] = {T(0), T(0), T(0)};
+    T rv[NV][3], rn[NV][3];
+    load_r(kf0, rv);
+    for (int kk = kf0; kk <= kf1; kk++) {
+        const bool ex = exists(kk);
+        const int k = wrapk(kk);
+        if (kk + 1 <= kf1) load_r(kk + 1, rn);   // in flight while plane kk is computed
+        copy_wait_but<1>();   // every group but the newest ({x of kk+2}) has landed
+        __syncthreads();      // ... for every thread; the residual plane is free
+        if (ex) {
+            const bool zin = g.zp || (k != 0 && k != g.o - 1);
+            const unsigned s0 = xslot(kk - 1), s1 = xslot(kk), s2 = xslot(kk + 1);
+            if (main) {
+#pragma unroll
+                for (int it = 0; it < 4; it++)
+                    rr_store<T, ELASTIC>(op.cop, s0, s1, s2, ii, kHalo + b + 2 * (pr0 + 4 * it), zin, rv[it], resp);
+            } else {
+#pragma unroll
+                for (int u = 0; u < kRRPer; u++) {
+                    int eii, ejj;
+                    if (enode(u, eii, ejj)) rr_store<T, ELASTIC>(op.cop, s0, s1, s2, eii, ejj, zin, rv[u], resp);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < NV; u++)
+#pragma unroll
+            for (int e = 0; e < 3; e++) rv[u][e] = rn[u][e];
+        __syncthreads();      // residual plane complete; x slot of plane kk - 1 free
+        if (kk + 3 <= kf1 + 1 && exists(kk + 3)) st.stage(g, x, wrapk(kk + 3), xslot(kk + 3));
+        copy_commit();
+        if (!main) continue;
+        if (kk & 1) {
+            // plane kk = 2K + 1 closes coarse plane K = (kk - 1) / 2 and opens K + 1
+            const int K = (kk - 1) >> 1;
+            const T w0 = ex && K >= K0 ? child_w<T>(K, kk, g.o, g.zp) : T(0);
+            const T w1 = ex && K + 1 < K1 ? child_w<T>(K + 1, kk, g.o, g.zp) : T(0);
+            T nxt[3] = {T(0), T(0), T(0)};
+            rr_add<T>(resp, ci, cj, w0, acc, w1, nxt);
+            if (K >= K0) {
+                const int p = slot(gc, Ic, Jc, K);
+                rc[p] = acc[0];
+                rc[p + gc.npad] = acc[1];
+                rc[p + 2 * gc.npad] = acc[2];
+            }
+            acc[0] = nxt[0];
+            acc[1] = nxt[1];
+            acc[2] = nxt[2];
+        } else {
+            const T w0 = ex ? child_w<T>(kk >> 1, kk, g.o, g.zp) : T(0);
+            rr_add<T>(resp, ci, cj, w0, acc, T(0), acc);
+        }
+    }
+    copy_wait_but<0>();
+}
+
+// Coarse planes per CTA of the fused kernel: about four waves of CTAs over
+// the SMs, 2 .. 16 coarse planes (each CTA also computes the fine plane below
+// its chunk).
+template <typename T>
+int rr_zc(const Geom &g, const Geom &gc) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long tiles = (long)(g.m / kTX) * (g.n / kTY);
+    const long per = 4L * sms * kMarchMinBlocks<T>;
+    const long z = (gc.o * tiles + per - 1) / per;
+    return (int)std::min<long>(16, std::max<long>(2, z));
+}
+
+template <typename T, bool ELASTIC>
+void launch_rr_k(const LevelOp<T> &op, const Geom &g, const Geom &gc, const T *r, const T *x, T *rc,
+                 cudaStream_t st) {
+    const int smem = kRRSmemWords * (int)sizeof(T);
+    const int zc = rr_zc<T>(g, gc);
+    const dim3 grid((g.m / kTX) * (g.n / kTY), (gc.o + zc - 1) / zc);
+    static unsigned long long attr_devices = 0;   // per instantiation
+    if (first_use_on_device(attr_devices))
+        cudaFuncSetAttribute(res_restrict_kernel<T, ELASTIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    res_restrict_kernel<T, ELASTIC><<<grid, kRRThreads, smem, st>>>(g, gc, op, r, x, rc, zc);
+}
+
 }  // namespace
 
 // Where the tiled sweep runs.  Measured on a GB300 (two sweeps, 256x256x257
@@ -648,6 +915,39 @@ void launch_residual_tile(const LevelOp<T> &op, const Geom &g, const T *r, const
         else launch_res_tile_k<T, OP_PLANE, false, false>(op, g, r, x, res, partial, st);
     }
 }
+
+// The descent's residual and restriction in one pass (res_restrict_kernel)
+// where the tiled residual runs on a shared-stencil level periodic in x and y
+// (an even z extent if z is periodic): rc = R (r - A x), res not written.
+// Opt-in (STZ_MG_FUSED_RESTRICT=1): measured on a GB300 at 256x256x257 it
+// saves the 404 MB of res traffic per cycle but is slower than the two
+// kernels (about 238 against 226 us per cycle, the mixed solve 23.0 against
+// 22.9 ms), because the marching residual is bound by the shared-memory pipe,
+// not by DRAM, and the restriction's loads (and the widened row and column)
+// add to that pipe.  False where it does not apply or is not enabled (the
+// caller runs the two kernels).
+template <typename T>
+bool launch_residual_restrict(const LevelOp<T> &op, const Geom &g, const Geom &gc, const T *r, const T *x, T *rc,
+                              cudaStream_t st) {
+    const char *e = std::getenv("STZ_MG_FUSED_RESTRICT");
+    if (!e || std::atoi(e) == 0) return false;
+    if (op.kind != OP_CONST || !residual_tile_applies(op, g)) return false;
+    if (g.zp && (g.o & 1)) return false;
+    if (gc.m * 2 != g.m || gc.n * 2 != g.n || !gc.xp || !gc.yp || gc.zp != g.zp) return false;
+    if (op.cop.elastic) {
+        launch_rr_k<T, true>(op, g, gc, r, x, rc, st);
+        return true;
+    }
+    if constexpr (sizeof(T) == 4) {   // a full-block row in FP64 would spill: the two kernels run instead
+        launch_rr_k<T, false>(op, g, gc, r, x, rc, st);
+        return true;
+    }
+    return false;
+}
+template bool launch_residual_restrict<float>(const LevelOp<float> &, const Geom &, const Geom &, const float *,
+                                              const float *, float *, cudaStream_t);
+template bool launch_residual_restrict<double>(const LevelOp<double> &, const Geom &, const Geom &, const double *,
+                                               const double *, double *, cudaStream_t);
 
 template bool residual_tile_applies<float>(const LevelOp<float> &, const Geom &);
 template bool residual_tile_applies<double>(const LevelOp<double> &, const Geom &);

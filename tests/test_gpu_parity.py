@@ -472,13 +472,15 @@ def test_band_kernels_fp64_solve_bitwise(dims, per, kind, bandres, monkeypatch):
                                           ((128, 64, 25), (True, True, False), "trans"),
                                           ((256, 256, 17), (True, True, False), "const")])
 def test_fused_residual_restriction_is_the_two_kernels(dims, per, kind, precision, monkeypatch):
-    """The descent's residual and restriction in one pass (the residual never
-    written) against the residual kernel followed by the restriction kernel:
-    the same cycle count and the same solution bit for bit, through whole
-    solves -- FP32 V-cycles of the mixed solver and FP64 ones (STZ_MG_TILE=1,
-    the tiled kernels in FP64 too), the elastic and a full non-symmetric
-    shared stencil, an odd and an even Dirichlet z (the even one puts the
-    last fine plane under the last coarse plane alone) and a periodic z."""
+    """The descent's residual and restriction in one pass (opt-in with
+    STZ_MG_FUSED_RESTRICT=1; the residual never written) against the
+    residual kernel followed by the restriction kernel:
+    the same iterate bit for bit after three V-cycles -- FP32 V-cycles of the
+    mixed solver and FP64 ones (STZ_MG_TILE=1, the tiled kernels in FP64
+    too), the elastic and a full non-symmetric shared stencil, an odd and an
+    even Dirichlet z (the even one puts the last fine plane under the last
+    coarse plane alone) and a periodic z (singular with x and y periodic:
+    GS at the bottom, no solve to a tolerance)."""
     import stzpp_gb300 as sg
     m, n, o = dims
     h = P.grid_spacing(m, n, o, per, h=1.0 / m)
@@ -489,11 +491,11 @@ def test_fused_residual_restriction_is_the_two_kernels(dims, per, kind, precisio
     out = {}
     for fused in ("0", "1"):
         monkeypatch.setenv("STZ_MG_FUSED_RESTRICT", fused)
-        with sg.Multigrid(dims, per, precision=precision, sweep_growth=False, v_down=2, v_up=2) as mg:
+        with sg.Multigrid(dims, per, precision=precision, sweep_growth=False, v_down=2, v_up=2, bottom="gs") as mg:
             mg.setup_matrices(stencil=st, fix=fix)
             mg.setup_fields(r=b)
-            cyc, rel = mg.solve(1e-10, 6, check=False)
-            out[fused] = (cyc, rel, mg.get_x())
-    assert np.isfinite(out["0"][1]) and out["0"][1] < 1e-2
-    assert out["0"][:2] == out["1"][:2]
-    assert np.array_equal(out["0"][2], out["1"][2])
+            for _ in range(3):
+                mg.v_cycle()
+            out[fused] = mg.get_x()
+    assert np.all(np.isfinite(out["0"])) and np.linalg.norm(out["0"]) > 0
+    assert np.array_equal(out["0"], out["1"])
