@@ -45,9 +45,18 @@ __device__ int g_band_err = 0;
 
 namespace {
 
-constexpr int kBandRows = 8;               // node rows of a band
-constexpr int kOwnSub = kBandRows / 2;     // sub-grid rows per parity owned by a band
-constexpr int kStageRows = kOwnSub + 2;    // staged sub-rows J0-1 .. J0+kOwnSub
+// Node rows of a band: 8 on every level.  Measured at 256x256x257 (mixed
+// solve, one box): 16-row bands on the 128x128 level 1 take its two sweeps
+// from 123 to 108 us timed alone, yet the solve from 22.79 to 22.85 ms (the
+// level's residual, and the launches around it, lose more); on the fine
+// level 16 rows leave one CTA per SM (371 against 337 us), on levels of
+// 16-32 columns they halve the CTAs of a launch (the solve 23.0 -> 23.6 ms);
+// 4 rows are slower everywhere (fine level 366 us).
+__host__ __device__ constexpr int band_rows(int) { return 8; }
+template <int M2>
+constexpr int kOwnSub = band_rows(M2) / 2;      // sub-grid rows per parity owned by a band
+template <int M2>
+constexpr int kStageRows = kOwnSub<M2> + 2;     // staged sub-rows J0-1 .. J0+kOwnSub
 
 // Shared-memory layout of the staged band: plane p (0: k-1, 1: k, 2: k+1),
 // component c, sub-row Jr (staged row 0 is sub-row J0-1), colour ab = a + 2b
@@ -55,10 +64,10 @@ constexpr int kStageRows = kOwnSub + 2;    // staged sub-rows J0-1 .. J0+kOwnSub
 // plane's component (all four colours of the staged sub-rows).
 template <int M2>
 __host__ __device__ constexpr int woff(int p, int c, int Jr, int ab, int I) {
-    return (((p * 3 + c) * kStageRows + Jr) * 4 + ab) * M2 + I;
+    return (((p * 3 + c) * kStageRows<M2> + Jr) * 4 + ab) * M2 + I;
 }
 template <int M2>
-constexpr int kBandWords = 3 * 3 * kStageRows * 4 * M2;
+constexpr int kBandWords = 3 * 3 * kStageRows<M2> * 4 * M2;
 
 template <int B, int E, typename F>
 __device__ __forceinline__ void sfor(F &&f) {
@@ -112,15 +121,16 @@ __device__ __forceinline__ void tma_load5(unsigned dst, const CUtensorMap *map, 
         : "memory");
 }
 
-// The tensor maps of one field (x_in or x_out): boxes of 6, 5 and 1 sub-rows.
+// The tensor maps of one field (x_in or x_out): boxes of kStageRows,
+// kStageRows - 1 and 1 sub-rows.
 struct BandMaps {
-    CUtensorMap rows6, rows5, rows1;
+    CUtensorMap full, less1, one;
 };
 
 struct BandArgs {
     Geom g;
     int c;          // plane parity of this launch
-    int nbands;     // n / kBandRows
+    int nbands;     // n / band_rows(M2)
     int nplanes;    // planes of parity c
     int rev;        // planes taken from the top down
     const void *xz; // the residual's x (read directly on Dirichlet plates)
@@ -139,13 +149,13 @@ __device__ __forceinline__ void stage_plane(const BandMaps &mp, const Geom &g, i
         const int cc = 2 * comp + cpar;
         // coordinates (I, ab, J, K, cc)
         if (J0 == 0) {   // rows N2-1 | 0 .. kOwnSub
-            tma_load5(dst, &mp.rows1, 0, 0, g.N2 - 1, K, cc, bar);
-            tma_load5(dst + rowb, &mp.rows5, 0, 0, 0, K, cc, bar);
-        } else if (J0 + kOwnSub == g.N2) {   // rows J0-1 .. N2-1 | 0
-            tma_load5(dst, &mp.rows5, 0, 0, J0 - 1, K, cc, bar);
-            tma_load5(dst + 5 * rowb, &mp.rows1, 0, 0, 0, K, cc, bar);
+            tma_load5(dst, &mp.one, 0, 0, g.N2 - 1, K, cc, bar);
+            tma_load5(dst + rowb, &mp.less1, 0, 0, 0, K, cc, bar);
+        } else if (J0 + kOwnSub<M2> == g.N2) {   // rows J0-1 .. N2-1 | 0
+            tma_load5(dst, &mp.less1, 0, 0, J0 - 1, K, cc, bar);
+            tma_load5(dst + (kStageRows<M2> - 1) * rowb, &mp.one, 0, 0, 0, K, cc, bar);
         } else {
-            tma_load5(dst, &mp.rows6, 0, 0, J0 - 1, K, cc, bar);
+            tma_load5(dst, &mp.full, 0, 0, J0 - 1, K, cc, bar);
         }
     }
 }
@@ -305,6 +315,7 @@ struct BandItem {
     bool zin, has_lo, has_hi;
 };
 
+template <int M2>
 __device__ __forceinline__ BandItem band_item(const BandArgs &args, int item) {
     const Geom &g = args.g;
     BandItem it;
@@ -312,7 +323,7 @@ __device__ __forceinline__ BandItem band_item(const BandArgs &args, int item) {
     const int kraw = item / args.nbands;
     it.K = args.rev ? args.nplanes - 1 - kraw : kraw;
     it.k = 2 * it.K + args.c;
-    it.J0 = it.band * kOwnSub;
+    it.J0 = it.band * kOwnSub<M2>;
     it.zin = g.zp || (it.k != 0 && it.k != g.o - 1);
     // planes k-1, k+1 exist (a Dirichlet z ends at the plates)
     it.has_lo = g.zp || it.k > 0;
@@ -351,8 +362,8 @@ __device__ __forceinline__ void band_plate(const Geom &g, const ConstOp<T> &op, 
     const size_t np = (size_t)g.npad;
     const T *inv = op.inv_fix;
 #pragma unroll 1
-    for (int w = hh; w < 4 * kOwnSub; w += NH) {
-        const int ab = w / kOwnSub, t = w % kOwnSub;
+    for (int w = hh; w < 4 * kOwnSub<M2>; w += NH) {
+        const int ab = w / kOwnSub<M2>, t = w % kOwnSub<M2>;
         const size_t sl = band_slot(g, ab, c, it.K, it.J0 + t, I);
         const T a0 = r[sl], a1 = r[sl + np], a2 = r[sl + 2 * np];
         xout[sl] = dot3(inv[0], a0, inv[1], a1, inv[2], a2);
@@ -374,9 +385,10 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
     const int c = args.c, K = it.K, J0 = it.J0, k = it.k;
     const size_t np = (size_t)g.npad;
     // this thread's rows of each colour
-    constexpr int P0 = kPer<kOwnSub + 1, NH>, P1 = kPer<kOwnSub, NH>;
+    constexpr int OWN = kOwnSub<M2>;
+    constexpr int P0 = kPer<OWN + 1, NH>, P1 = kPer<OWN, NH>;
     const int t0a = hh * P0, t0b = hh * P1;
-    const int na = min(P0, kOwnSub + 1 - t0a), nb = min(P1, kOwnSub - t0b);
+    const int na = min(P0, OWN + 1 - t0a), nb = min(P1, OWN - t0b);
     T r0[P0][3], r1[P0][3], r2[P1][3], r3[P1][3];
 #pragma unroll
     for (int u = 0; u < P0; u++) {
@@ -434,7 +446,7 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
             if (to_smem)
 #pragma unroll
                 for (int cc = 0; cc < 3; cc++) s[I + woff<M2>(1, cc, 0, A + 2 * B, 0) + (t + 1) * rowstep] = o[u][cc];
-            if (t < kOwnSub) {
+            if (t < OWN) {
                 const size_t sl = band_slot(g, A + 2 * B, c, K, J0 + t, I);
 #pragma unroll
                 for (int cc = 0; cc < 3; cc++) xout[sl + cc * np] = o[u][cc];
@@ -472,15 +484,22 @@ __device__ __forceinline__ bool band_compute(const BandArgs &args, const LevelOp
 }
 
 // One CTA per work item.
+// CTAs per SM the sweep's registers must allow: on the widest FP32 level as
+// many as the staging buffer lets share an SM's 228 KB (two of 110.6 KB with
+// 8-row bands); one elsewhere (ptxas then keeps every value in registers).
+template <typename T, int M2, int KIND>
+constexpr int kBandMinBlocks =
+    sizeof(T) == 4 && M2 >= 128 ? (KIND == OP_CONST ? 233472 / (kBandWords<M2> * 4 + 2048) : 2) : 1;
+
 template <typename T, int M2, int NH, int KIND, bool SPARSE>
-__global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
+__global__ void __launch_bounds__(NH * M2, (kBandMinBlocks<T, M2, KIND>))
     gs_band_kernel(const BandArgs args, const __grid_constant__ LevelOp<T> op, const __grid_constant__ BandMaps in,
                    const __grid_constant__ BandMaps out_maps, const T *__restrict__ r, T *__restrict__ xout) {
     extern __shared__ __align__(128) unsigned char band_smem[];
     __shared__ __align__(8) unsigned long long bar_store;
     __shared__ __align__(16) T cfs[KIND == OP_PLANE ? kCoefWords : 4];
     const int tid = threadIdx.x;
-    const BandItem it = band_item(args, blockIdx.x);
+    const BandItem it = band_item<M2>(args, blockIdx.x);
     if (!band_stages<KIND>(it)) {
         band_plate<T, M2, NH>(args.g, op.cop, it, args.c, r, xout);
         return;
@@ -615,13 +634,13 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
     const Geom &g = args.g;
     const int tid = threadIdx.x, I = tid % M2, hh = tid / M2;
     const int band = blockIdx.x % args.nbands, k = blockIdx.x / args.nbands;
-    const int c = k & 1, K = k >> 1, J0 = band * kOwnSub;
+    const int c = k & 1, K = k >> 1, J0 = band * kOwnSub<M2>;
     const size_t np = (size_t)g.npad;
     const bool has_lo = g.zp || k > 0, has_hi = g.zp || k < g.o - 1;
     if (KIND == OP_CONST && !(has_lo && has_hi)) {   // a Dirichlet plate: r - fix x
 #pragma unroll 1
-        for (int w = hh; w < 4 * kOwnSub; w += NH) {
-            const int ab = w / kOwnSub, t = w % kOwnSub;
+        for (int w = hh; w < 4 * kOwnSub<M2>; w += NH) {
+            const int ab = w / kOwnSub<M2>, t = w % kOwnSub<M2>;
             const size_t sl = band_slot(g, ab, c, K, J0 + t, I);
             T acc[3] = {r[sl], r[sl + np], r[sl + 2 * np]};
             const T *xp = static_cast<const T *>(args.xz);
@@ -671,8 +690,8 @@ __global__ void __launch_bounds__(NH * M2, sizeof(T) == 4 && M2 >= 128 ? 2 : 1)
             for (int w = tid; w < PW; w += NH * M2) s[2 * PW + w] = T(0);
         __syncthreads();
     }
-    constexpr int P = kPer<kOwnSub, NH>;
-    const int t0 = hh * P, nv = min(P, kOwnSub - t0);
+    constexpr int P = kPer<kOwnSub<M2>, NH>;
+    const int t0 = hh * P, nv = min(P, kOwnSub<M2> - t0);
     const int ib[3] = {I == 0 ? M2 - 1 : I - 1, I, I == M2 - 1 ? 0 : I + 1};
     // the four colours as the branches of a loop that is not unrolled: the
     // colours share no barrier, and in one straight run the instruction
@@ -724,8 +743,9 @@ bool make_band_maps(const Geom &g, const T *field, BandMaps &mp) {
     const cuuint64_t dims[5] = {M2, 4, N2, O2, 6}, strides[4] = {S * e, M2 * e, M2 * N2 * e, 4 * S * e};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-    CUtensorMap *maps[3] = {&mp.rows6, &mp.rows5, &mp.rows1};
-    const cuuint32_t rows[3] = {kStageRows, kStageRows - 1, 1};
+    CUtensorMap *maps[3] = {&mp.full, &mp.less1, &mp.one};
+    const cuuint32_t stage = (cuuint32_t)(band_rows(g.M2) / 2 + 2);
+    const cuuint32_t rows[3] = {stage, stage - 1, 1};
     for (int i = 0; i < 3; i++) {
         const cuuint32_t box[5] = {(cuuint32_t)M2, 4, rows[i], 1, 1};
         if (enc(maps[i], dt, 5, const_cast<T *>(field), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -761,7 +781,7 @@ bool launch_band_kn(const LevelOp<T> &op, const Geom &g, const T *r, const T *xi
     if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     BandArgs a;
     a.g = g;
-    a.nbands = g.n / kBandRows;
+    a.nbands = g.n / band_rows(g.M2);
     a.xz = nullptr;
     for (int c = 0; c < 2; c++) {
         const int planes = c == 0 ? (g.o + 1) / 2 : g.o / 2;
@@ -779,12 +799,12 @@ bool launch_band_kn(const LevelOp<T> &op, const Geom &g, const T *r, const T *xi
 
 // Threads per column of the sweep: in FP32 two on wide levels (64 or 128
 // sub-grid columns; four, with twice the warps, measured no faster: 350 vs
-// 347 us for two fine sweeps, 131 vs 126 us on level 1, where a thread's
-// three rows share each coefficient load) and four on narrow ones (few nodes
-// per row); one or two in FP64 (shared memory and registers).
+// 347 us for two fine sweeps with 8-row bands, 131 vs 126 us on level 1,
+// where a thread's rows share each coefficient load) and four on narrow
+// ones (few nodes per row); one or two in FP64 (registers).
 template <typename T, int M2, int KIND, bool SPARSE>
 bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
-    constexpr int NH = sizeof(T) == 8 ? (M2 >= 64 ? 1 : 2) : (M2 >= 64 ? 2 : 4);
+    constexpr int NH = sizeof(T) == 4 ? (M2 >= 64 ? 2 : 4) : (M2 >= 64 ? 1 : 2);
     return launch_band_kn<T, M2, NH, KIND, SPARSE>(op, g, r, xin, xout, st);
 }
 
@@ -821,7 +841,8 @@ bool gs_band_applies(const LevelOp<T> &op, const Geom &g) {
     if (mode == 0) return false;
     if (mode < 0 && sizeof(T) != 4) return false;
     if (!((op.kind == OP_CONST && op.cop.elastic) || op.kind == OP_PLANE)) return false;
-    if (!g.xp || !g.yp || (g.m & 1) || g.n % kBandRows != 0 || g.n < 2 * kBandRows) return false;
+    const int rows = band_rows(g.M2);
+    if (!g.xp || !g.yp || (g.m & 1) || g.n % rows != 0 || g.n < 2 * rows) return false;
     if (g.M2 != 8 && g.M2 != 16 && g.M2 != 32 && g.M2 != 64 && g.M2 != 128) return false;
     if (g.zp && (g.o & 1)) return false;
     return true;
@@ -847,7 +868,7 @@ bool launch_res_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T 
     if (first_band_use(attr_devices)) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     BandArgs a;
     a.g = g;
-    a.nbands = g.n / kBandRows;
+    a.nbands = g.n / band_rows(g.M2);
     a.c = 0;
     a.nplanes = g.o;
     a.rev = 0;

@@ -324,11 +324,12 @@ def test_tiled_sweep_mixed_solve_bitwise(dims, per, kind, monkeypatch):
 
 BAND_LEVEL_CASES = [((64, 64, 17), (True, True, False), "const", 0, 2), ((64, 64, 16), (True, True, True), "const", 0, 2),
                     ((128, 64, 9), (True, True, False), "const", 0, 3), ((128, 128, 8), (True, True, True), "const", 0, 2),
-                    ((256, 256, 9), (True, True, False), "const", 0, 2), ((64, 16, 5), (True, True, False), "const", 0, 4),
+                    ((256, 256, 9), (True, True, False), "const", 0, 2), ((64, 32, 5), (True, True, False), "const", 0, 4),
                     ((128, 128, 17), (True, True, False), "const", 1, 2), ((128, 128, 16), (True, True, True), "const", 1, 3),
                     ((128, 64, 17), (True, True, False), "trans", 1, 2), ((256, 128, 10), (True, True, False), "trans", 1, 2),
                     ((32, 32, 17), (True, True, False), "const", 0, 2), ((16, 16, 9), (True, True, False), "const", 0, 3),
-                    ((64, 64, 33), (True, True, False), "const", 1, 2), ((64, 32, 16), (True, True, True), "trans", 1, 2)]
+                    ((64, 64, 33), (True, True, False), "const", 1, 2), ((64, 64, 16), (True, True, True), "trans", 1, 2),
+                    ((128, 32, 9), (True, True, False), "const", 0, 3), ((256, 64, 12), (True, True, True), "trans", 1, 2)]
 
 
 @pytest.mark.parametrize("dims,per,kind,level,sweeps", BAND_LEVEL_CASES)
