@@ -935,18 +935,23 @@ double rhs_norm(stz_mg_handle h);
 // The residual of the mixed solver's correction steps (r32 non-null): in
 // double-float arithmetic on a shared-stencil top level (residual_df.cu),
 // with x split into float pairs in the FP64 level's res field (scratch: the
-// calls that report a residual recompute it there) -- else in FP64.
-// Returns |b - A x|^2 in FP64.
-double top_residual_sq(stz_mg_handle h, float *r32) {
+// calls that report a residual recompute it there) -- else in FP64.  With
+// corr non-null the correction x += corr is applied first (in the split's
+// pass where the double-float residual runs).  Returns |b - A x|^2 in FP64.
+double top_residual_sq(stz_mg_handle h, float *r32, const float *corr = nullptr) {
     const Geom &g = h->geo[0];
     double unscale = 1.0;
     if (r32 && residual_df_applies(h->op64[0])) {
         const double bn = rhs_norm(h);
         const double scale = df_norm_scale(bn * bn, 3 * npts(g));
-        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, reinterpret_cast<float2 *>(h->L64[0].res), r32,
-                           scale, h->partial, h->dscal, h->st);
+        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, corr, reinterpret_cast<float2 *>(h->L64[0].res),
+                           r32, scale, h->partial, h->dscal, h->st);
         unscale = 1.0 / (scale * scale);
         h->stat_launches += 1;   // the split of x
+    } else if (corr) {
+        launch_add_correction(h->L64[0].x, corr, 3 * (size_t)g.npad, h->st);
+        h->stat_launches += 1;
+        return top_residual_sq(h, r32);
     } else if (r32) {
         launch_residual<double, float>(h->op64[0], g, h->L64[0].r, h->L64[0].x, r32, h->partial, h->dscal, h->st);
     } else {
@@ -997,12 +1002,14 @@ bool top_x_is_zero(stz_mg_handle h) {
 
 // One mixed-precision defect-correction step with k FP32 V-cycles:
 // r32 = b - A x (FP64 residual rounded to FP32), e = 0, k cycles on A e = r32,
-// x += e in FP64.
-void mixed_step(stz_mg_handle h, int k) {
+// x += e in FP64 -- here, or (apply false) by the caller's next
+// top_residual_sq(h, r32, e).
+void mixed_step(stz_mg_handle h, int k, bool apply = true) {
     const Geom &g = h->geo[0];
     const size_t n3 = 3 * (size_t)g.npad;
     CK(cudaMemsetAsync(h->L32[0].x, 0, n3 * sizeof(float), h->st));
     run_vcycle32(h, k);
+    if (!apply) return;
     launch_add_correction(h->L64[0].x, h->L32[0].x, n3, h->st);
     check_launch();
     h->stat_launches += 1;
@@ -1042,9 +1049,9 @@ void solve(stz_mg_handle h, double tol, int max_cycles, int *cycles_out, double 
         const bool trace = std::getenv("STZ_MG_TRACE") != nullptr;
         while (rn > target && cycles < max_cycles) {
             k = std::max(1, std::min(k, max_cycles - cycles));
-            mixed_step(h, k);
+            mixed_step(h, k, false);   // x += e in the residual's first pass
             cycles += k;
-            rsq = top_residual_sq(h, h->L32[0].r);
+            rsq = top_residual_sq(h, h->L32[0].r, h->L32[0].x);
             double rn_new = std::sqrt(rsq);
             if (trace) fprintf(stderr, "stz_mg mixed: %d cycles, |r|/|b| %.3e -> %.3e\n", k, rn / bn, rn_new / bn);
             double gain = rn_new / rn;
@@ -1787,7 +1794,7 @@ int stz_mg_time_kernel(stz_mg_handle h, int kernel, int level, int reps, double 
                     // the mixed solver's pass: split of x + double-float residual + sum
                     const double scale = df_norm_scale(rhs_norm(h) * rhs_norm(h), 3 * npts(g));
                     launch = [&, scale] {
-                        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x,
+                        launch_residual_df(h->op64[0], g, h->L64[0].r, h->L64[0].x, nullptr,
                                            reinterpret_cast<float2 *>(h->L64[0].res), h->L32[0].r, scale, h->partial,
                                            h->dscal, h->st);
                     };

@@ -82,12 +82,13 @@ int residual_blocks(const Geom &g);
 void launch_sum_partials(const double *partial, int n, double *out, cudaStream_t st);
 // residual_df.cu: r32 = b - A x of a shared-stencil top level in double-float
 // arithmetic (x split first into the (hi, lo) float pairs xs, 3*npad of
-// them); per-block sums of (scale * r32)^2 into partial and, when out is
-// non-null, their sum to out[0]
+// them; with corr non-null x += corr first, in the same pass); per-block
+// sums of (scale * r32)^2 into partial and, when out is non-null, their sum
+// to out[0]
 bool residual_df_applies(const LevelOp<double> &op);
 double df_norm_scale(double bsq, size_t n);
-void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, const double *x, float2 *xs,
-                        float *r32, double scale, double *partial, double *out, cudaStream_t st);
+void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, double *x, const float *corr,
+                        float2 *xs, float *r32, double scale, double *partial, double *out, cudaStream_t st);
 // res = r - A x (res may be null); when partial is non-null, per-block sums of
 // |res|^2 go to partial[residual_blocks(g)] and, when out is non-null, their
 // total to out[0].

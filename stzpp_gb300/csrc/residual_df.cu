@@ -111,10 +111,28 @@ __device__ __forceinline__ void df_sub_prod(float &sh, float &sl, float ah, floa
     sl = __fsub_rn(__fadd_rn(sl, __fsub_rn(err, ep)), cross);
 }
 
-__global__ void split_kernel(const double *__restrict__ x, float2 *__restrict__ xs, size_t n) {
+// (sh, sl) = (ah, al)-free sum of two pairs: (xh1 + xl1) + (xh2 + xl2) with
+// the high parts' sum exact (two-sum) and every rounding error in the low part.
+__device__ __forceinline__ void df_add(float xh1, float xl1, float xh2, float xl2, float &sh, float &sl) {
+    const float s = __fadd_rn(xh1, xh2);
+    const float bv = __fsub_rn(s, xh1);
+    const float err = __fadd_rn(__fsub_rn(xh1, __fsub_rn(s, bv)), __fsub_rn(xh2, bv));
+    sh = s;
+    sl = __fadd_rn(__fadd_rn(xl1, xl2), err);
+}
+
+// xs = x split into pairs; with e non-null x += e first (the defect
+// correction's update, add_correction_kernel's arithmetic) and written back.
+__global__ void split_kernel(double *__restrict__ x, const float *__restrict__ e, float2 *__restrict__ xs,
+                             size_t n) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        double xv = x[t];
+        if (e) {
+            xv += (double)e[t];
+            x[t] = xv;
+        }
         float2 v;
-        split_double(x[t], v.x, v.y);
+        split_double(xv, v.x, v.y);
         xs[t] = v;
     }
 }
@@ -123,7 +141,7 @@ __global__ void split_kernel(const double *__restrict__ x, float2 *__restrict__ 
 // per block, the FP64 sum of (scale * r32)^2 into partial; xs: x as
 // (hi, lo) pairs.  Thread layout of residual_kernel: block (32, 8), lanes
 // along x, threadIdx.y the colour.
-template <bool ELASTIC, bool AL>
+template <bool ELASTIC, bool AL, bool PAIRED>
 __global__ void __launch_bounds__(kDfThreads) residual_df_kernel(Geom g, const __grid_constant__ DfConst op,
                                                                  int centre_diag, const double *__restrict__ b,
                                                                  const float2 *__restrict__ xs,
@@ -142,7 +160,42 @@ __global__ void __launch_bounds__(kDfThreads) residual_df_kernel(Geom g, const _
             float sh[3], sl[3];
 #pragma unroll
             for (int cc = 0; cc < 3; cc++) split_double(b[p + cc * np], sh[cc], sl[cc]);
-            if (is_interior(g, i, j, k)) {
+            if (PAIRED && is_interior(g, i, j, k)) {
+                // blocks d and -d carry the same coefficients: one product per
+                // pair, of the neighbours' double-float sum
+                const NbrOffsets nb = nbr_offsets_sub(g, I, J, K, a, bq, c);
+#pragma unroll
+                for (int blk = 0; blk < 27; blk++) {
+                    if (blk > 13 || (ELASTIC && nnz_axes(blk) == 3)) continue;
+                    const int mblk = 26 - blk;
+                    const int s0 = nb.ox[bdx(blk) + 1] + nb.oy[bdy(blk) + 1] + nb.oz[bdz(blk) + 1];
+                    const int s1 = nb.ox[bdx(mblk) + 1] + nb.oy[bdy(mblk) + 1] + nb.oz[bdz(mblk) + 1];
+                    float vh[3], vl[3];
+#pragma unroll
+                    for (int cc = 0; cc < 3; cc++) {
+                        bool used = !ELASTIC || blk == 13;
+#pragma unroll
+                        for (int rr = 0; rr < 3; rr++) used = used || elastic_entry(blk, 3 * rr + cc);
+                        if (!used) {
+                            vh[cc] = vl[cc] = 0.0f;
+                        } else if (blk == 13) {
+                            const float2 v = xs[s0 + cc * np];
+                            vh[cc] = v.x;
+                            vl[cc] = v.y;
+                        } else {
+                            const float2 v0 = xs[s0 + cc * np], v1 = xs[s1 + cc * np];
+                            df_add(v0.x, v0.y, v1.x, v1.y, vh[cc], vl[cc]);
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < 9; e++) {
+                        if (ELASTIC && blk != 13 && !elastic_entry(blk, e)) continue;
+                        if (blk == 13 && centre_diag && e % 4 != 0) continue;   // warp-uniform
+                        if (!ELASTIC && op.ah[blk][e] == 0.0f) continue;      // warp-uniform
+                        df_sub_prod<AL>(sh[e / 3], sl[e / 3], op.ah[blk][e], op.al[blk][e], vh[e % 3], vl[e % 3]);
+                    }
+                }
+            } else if (is_interior(g, i, j, k)) {
                 const NbrOffsets nb = nbr_offsets_sub(g, I, J, K, a, bq, c);
 #pragma unroll
                 for (int blk = 0; blk < 27; blk++) {
@@ -220,10 +273,26 @@ DfConst split_stencil(const ConstOp<double> &op, bool *exact) {
 }
 
 template <bool ELASTIC, bool AL>
-void launch_df(const Geom &g, const DfConst &d, int centre_diag, const double *b, const float2 *xs, float *r32,
-               float scale, double *partial, cudaStream_t st) {
+void launch_df(const Geom &g, const DfConst &d, bool paired, int centre_diag, const double *b, const float2 *xs,
+               float *r32, float scale, double *partial, cudaStream_t st) {
     const dim3 blocks((g.M2 + 31) / 32, g.N2, g.O2), blk(32, 8);
-    residual_df_kernel<ELASTIC, AL><<<blocks, blk, 0, st>>>(g, d, centre_diag, b, xs, r32, scale, partial);
+    if (paired)
+        residual_df_kernel<ELASTIC, AL, true><<<blocks, blk, 0, st>>>(g, d, centre_diag, b, xs, r32, scale, partial);
+    else
+        residual_df_kernel<ELASTIC, AL, false><<<blocks, blk, 0, st>>>(g, d, centre_diag, b, xs, r32, scale, partial);
+}
+
+// Whether every block d of the stencil equals block -d (a symmetric shared
+// stencil whose blocks are symmetric, as the elasticity stencil's are):
+// then the residual forms one product per pair of opposite neighbours.
+// STZ_MG_DF_PAIRS=0 turns the pairing off.
+bool stencil_paired(const ConstOp<double> &op) {
+    if (const char *e = std::getenv("STZ_MG_DF_PAIRS"))
+        if (std::atoi(e) == 0) return false;
+    for (int blk = 0; blk < 13; blk++)
+        for (int e = 0; e < 9; e++)
+            if (op.a[blk][e] != op.a[26 - blk][e]) return false;
+    return true;
 }
 
 }  // namespace
@@ -245,21 +314,22 @@ double df_norm_scale(double bsq, size_t n) {
     return std::ldexp(1.0, -(e < -120 ? -120 : (e > 120 ? 120 : e)));   // a normal float
 }
 
-void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, const double *x, float2 *xs,
-                        float *r32, double scale, double *partial, double *out, cudaStream_t st) {
+void launch_residual_df(const LevelOp<double> &op, const Geom &g, const double *b, double *x, const float *corr,
+                        float2 *xs, float *r32, double scale, double *partial, double *out, cudaStream_t st) {
     const size_t n = 3 * (size_t)g.npad;
     const unsigned sb = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32);
-    split_kernel<<<sb, 256, 0, st>>>(x, xs, n);
+    split_kernel<<<sb, 256, 0, st>>>(x, corr, xs, n);
     bool exact = false;
     const DfConst d = split_stencil(op.cop, &exact);
     const int cd = op.cop.centre_diag;
     const float sc = (float)scale;
+    const bool pr = stencil_paired(op.cop);
     if (op.cop.elastic) {
-        if (exact) launch_df<true, false>(g, d, cd, b, xs, r32, sc, partial, st);
-        else launch_df<true, true>(g, d, cd, b, xs, r32, sc, partial, st);
+        if (exact) launch_df<true, false>(g, d, pr, cd, b, xs, r32, sc, partial, st);
+        else launch_df<true, true>(g, d, pr, cd, b, xs, r32, sc, partial, st);
     } else {
-        if (exact) launch_df<false, false>(g, d, cd, b, xs, r32, sc, partial, st);
-        else launch_df<false, true>(g, d, cd, b, xs, r32, sc, partial, st);
+        if (exact) launch_df<false, false>(g, d, pr, cd, b, xs, r32, sc, partial, st);
+        else launch_df<false, true>(g, d, pr, cd, b, xs, r32, sc, partial, st);
     }
     if (out) launch_sum_partials(partial, residual_blocks(g), out, st);
 }
