@@ -230,28 +230,50 @@ __device__ __forceinline__ void band_colour(const T *__restrict__ s, const int (
         for (int u = 0; u < NR; u++)
 #pragma unroll
             for (int e = 0; e < 3; e++) acc[u][e] = rr[u][e];
-        sfor<0, 27>([&](auto bi) {
-            constexpr int b = decltype(bi)::value;
-            if constexpr (b != 13) {
-                constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
-                constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
-                constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
-                asm volatile("" ::: "memory");
-                T cb[kCoefPad];
-                load_block_coef<T>(cf + kCoefPad * b, cb);
+        // one block: its coefficients at cf + kCoefPad * b, its neighbours in
+        // buffer plane 1 + dz (shared-memory offset pz of that plane)
+        auto block = [&](auto bi, int b, int pz) {
+            constexpr int bxy = decltype(bi)::value;   // dx + 1 + 3 (dy + 1)
+            constexpr int dx = bxy % 3 - 1, dy = bxy / 3 - 1;
+            constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
+            constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
+            asm volatile("" ::: "memory");
+            T cb[kCoefPad];
+            load_block_coef<T>(cf + kCoefPad * b, cb);
 #pragma unroll
-                for (int u = 0; u < NR; u++) {
-                    const int base = ib[sI + 1] + roff[u] + sJ * rowstep;
-                    T v[3];
-                    v[0] = s[base + woff<M2>(1 + dz, 0, 0, ap + 2 * bp, 0)];
-                    v[1] = s[base + woff<M2>(1 + dz, 1, 0, ap + 2 * bp, 0)];
-                    v[2] = s[base + woff<M2>(1 + dz, 2, 0, ap + 2 * bp, 0)];
+            for (int u = 0; u < NR; u++) {
+                const int base = ib[sI + 1] + roff[u] + sJ * rowstep + pz;
+                T v[3];
+                v[0] = s[base + woff<M2>(0, 0, 0, ap + 2 * bp, 0)];
+                v[1] = s[base + woff<M2>(0, 1, 0, ap + 2 * bp, 0)];
+                v[2] = s[base + woff<M2>(0, 2, 0, ap + 2 * bp, 0)];
 #pragma unroll
-                    for (int e = 0; e < 9; e++)
-                        if (!SPARSE || coarse_entry(b, e)) acc[u][e / 3] -= cb[e] * v[e % 3];
-                }
+                for (int e = 0; e < 9; e++)
+                    if (!SPARSE || coarse_entry(b, e)) acc[u][e / 3] -= cb[e] * v[e % 3];
             }
-        });
+        };
+        if constexpr (SPARSE) {
+            // the structural zeros depend on the block: every block unrolled
+            sfor<0, 27>([&](auto bi) {
+                constexpr int b = decltype(bi)::value;
+                if constexpr (b != 13)
+                    block(std::integral_constant<int, b % 9>{}, b, (bdz(b) + 1) * woff<M2>(1, 0, 0, 0, 0));
+            });
+        } else {
+            // the three planes of blocks in turn (blocks in ascending order,
+            // as plane_row_coef takes them), the nine of a plane unrolled: a
+            // third of the code of the whole unrolled row, which stalled on
+            // instruction fetch (level 1, two sweeps: 123 -> 115 us; the
+            // mixed solve 22.64 -> 22.03 ms)
+#pragma unroll 1
+            for (int dz = 0; dz < 3; dz++) {
+                const int pz = dz * woff<M2>(1, 0, 0, 0, 0);
+                sfor<0, 9>([&](auto bi) {
+                    constexpr int bxy = decltype(bi)::value;
+                    if (dz != 1 || bxy != 4) block(bi, 9 * dz + bxy, pz);   // not the centre
+                });
+            }
+        }
         T inv[kCoefPad];
         load_block_coef<T>(cf + kCoefPad * 27, inv);
 #pragma unroll
@@ -548,9 +570,11 @@ __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const i
             acc[u][1] = r[sl + np];
             acc[u][2] = r[sl + 2 * np];
         }
-        sfor<0, 27>([&](auto bi) {
-            constexpr int b = decltype(bi)::value;
-            constexpr int dx = bdx(b), dy = bdy(b), dz = bdz(b);
+        // one block (as in band_colour), the planes of blocks rolled where
+        // no structural zeros are skipped
+        auto block = [&](auto bi, int b, int pz) {
+            constexpr int bxy = decltype(bi)::value;
+            constexpr int dx = bxy % 3 - 1, dy = bxy / 3 - 1;
             constexpr int ap = (A + dx + 2) & 1, sI = (A + dx + 2) / 2 - 1;
             constexpr int bp = (B + dy + 2) & 1, sJ = (B + dy + 2) / 2 - 1;
             asm volatile("" ::: "memory");
@@ -558,16 +582,28 @@ __device__ __forceinline__ void band_res_colour(const T *__restrict__ s, const i
             load_block_coef<T>(cf + kCoefPad * b, cb);
 #pragma unroll
             for (int u = 0; u < NR; u++) {
-                const int base = ib[sI + 1] + roff[u] + sJ * rowstep;
+                const int base = ib[sI + 1] + roff[u] + sJ * rowstep + pz;
                 T v[3];
-                v[0] = s[base + woff<M2>(1 + dz, 0, 0, ap + 2 * bp, 0)];
-                v[1] = s[base + woff<M2>(1 + dz, 1, 0, ap + 2 * bp, 0)];
-                v[2] = s[base + woff<M2>(1 + dz, 2, 0, ap + 2 * bp, 0)];
+                v[0] = s[base + woff<M2>(0, 0, 0, ap + 2 * bp, 0)];
+                v[1] = s[base + woff<M2>(0, 1, 0, ap + 2 * bp, 0)];
+                v[2] = s[base + woff<M2>(0, 2, 0, ap + 2 * bp, 0)];
 #pragma unroll
                 for (int e = 0; e < 9; e++)
                     if (!SPARSE || coarse_entry(b, e)) acc[u][e / 3] -= cb[e] * v[e % 3];
             }
-        });
+        };
+        if constexpr (SPARSE) {
+            sfor<0, 27>([&](auto bi) {
+                constexpr int b = decltype(bi)::value;
+                block(std::integral_constant<int, b % 9>{}, b, (bdz(b) + 1) * woff<M2>(1, 0, 0, 0, 0));
+            });
+        } else {
+#pragma unroll 1
+            for (int dz = 0; dz < 3; dz++) {
+                const int pz = dz * woff<M2>(1, 0, 0, 0, 0);
+                sfor<0, 9>([&](auto bi) { block(bi, 9 * dz + decltype(bi)::value, pz); });
+            }
+        }
 #pragma unroll
         for (int u = 0; u < NR; u++)
             if (u < nv) {
