@@ -223,6 +223,17 @@ void check_level(stz_mg_handle h, int l) {
 }
 
 // ------------------------------------------------------------ hierarchy
+// The 8-colour smoother needs every periodic dimension even (or 1): an odd
+// periodic dimension would couple two nodes of the same colour.
+bool odd_periodic(int m, int n, int o, int xp, int yp, int zp) {
+    return (xp && m > 1 && (m & 1)) || (yp && n > 1 && (n & 1)) || (zp && o > 1 && (o & 1));
+}
+
+// multigrid::multigrid's hierarchy (multigrid.cc:40): coarsen until a level
+// has at most max_coarse nodes.  Where the next level would have an odd
+// periodic dimension (a periodic size whose halving chain reaches an odd
+// size above max_coarse, e.g. 72 -> 36 -> 18 -> 9), the hierarchy stops at
+// the last even level instead, which then is the bottom level.
 void build_geometry(stz_mg_handle h) {
     const stz_mg_desc &d = h->d;
     h->geo[0] = make_geom(d.m, d.n, d.o, d.x_prd, d.y_prd, d.z_prd);
@@ -231,14 +242,13 @@ void build_geometry(stz_mg_handle h) {
         const Geom &P = h->geo[h->nlev - 1];
         int mc = (P.m + (P.xp ? 1 : 2)) >> 1, nc = (P.n + (P.yp ? 1 : 2)) >> 1, oc = (P.o + (P.zp ? 1 : 2)) >> 1;
         if (mc == P.m && nc == P.n && oc == P.o) break;
+        if (odd_periodic(mc, nc, oc, P.xp, P.yp, P.zp)) break;
         if (h->nlev == kMaxLev) fail(STZ_MG_ERR_UNSUPPORTED, "more than %d levels", kMaxLev);
         h->geo[h->nlev++] = make_geom(mc, nc, oc, P.xp, P.yp, P.zp);
     }
-    // The 8-colour smoother needs every periodic dimension even (or 1): an odd
-    // periodic dimension would couple two nodes of the same colour.
     for (int l = 0; l < h->nlev; l++) {
         const Geom &g = h->geo[l];
-        if ((g.xp && g.m > 1 && (g.m & 1)) || (g.yp && g.n > 1 && (g.n & 1)) || (g.zp && g.o > 1 && (g.o & 1)))
+        if (odd_periodic(g.m, g.n, g.o, g.xp, g.yp, g.zp))
             fail(STZ_MG_ERR_UNSUPPORTED,
                  "level %d has an odd periodic dimension (%dx%dx%d); the 8-colour smoother needs even periodic sizes",
                  l, g.m, g.n, g.o);

@@ -504,3 +504,34 @@ def test_fused_residual_restriction_is_the_two_kernels(dims, per, kind, precisio
             out[fused] = mg.get_x()
     assert np.all(np.isfinite(out["0"])) and np.linalg.norm(out["0"]) > 0
     assert np.array_equal(out["0"], out["1"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_hierarchy_stops_before_an_odd_periodic_level(precision, oracle_port):
+    """72x72x17, periodic x and y: the halving chain 72 -> 36 -> 18 -> 9 would
+    reach an odd periodic size above max_coarse (18x18x5 = 1620 nodes), which
+    the 8-colour smoother cannot take; the hierarchy stops at 18x18x5, and
+    the converged solution matches the reference's lexicographic solver with
+    its own hierarchy (which goes on to 9x9x3)."""
+    import stzpp_gb300 as sg
+    dims, per = (72, 72, 17), (True, True, False)
+    m, n, o = dims
+    dx, dy, dz = P.grid_spacing(m, n, o, per, h=1.0 / m)   # isotropic: the cycles converge
+    b = P.rhs_divergence(P.random_strain(0, m, n, o, per), m, n, o, per, dx, dy, dz)
+    st, fix = P.elastic_stencil_const(1.0, 2.0, dx, dy, dz)
+    ref = oracle_port.PortMultigrid(dims, per, stencil=st, fix=fix, max_coarse=1024)
+    ref.set_field(0, "r", b)
+    ref.set_field(0, "x", np.zeros_like(b))
+    cyc_ref, hist = ref.solve(1e-13, 100, bottom="gs", smoother="lex")
+    assert hist[cyc_ref - 1] <= 1e-13
+    x_ref = ref.get_field(0, "x")
+    with sg.Multigrid(dims, per, precision=precision) as mg:
+        assert mg.nlevels == 3
+        assert mg.level_npts(2) == 18 * 18 * 5
+        mg.setup_matrices(*sg.elastic_stencil(1.0, 2.0, dx, dy, dz))
+        mg.setup_fields(r=b)
+        cycles, rel = mg.solve(1e-10, 100)
+        x = mg.get_x()
+    assert rel <= 1e-10
+    err = np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)
+    assert err <= SOLUTION_RTOL, f"{precision}: {cycles} cycles, error {err:.3e}"
