@@ -1,9 +1,11 @@
-// Band Gauss-Seidel sweep of the fine level: the 8-colour sweep of a shared
-// elasticity stencil on a level periodic in x and y, two launches per sweep,
-// every CTA staging its planes with the tensor-memory-access (TMA) engine.
+// Band Gauss-Seidel sweep of the levels periodic in x and y -- the fine
+// level's shared elasticity stencil and the plane-invariant coarse operators
+// below it -- two launches per sweep, every CTA staging its planes with the
+// tensor-memory-access (TMA) engine; and the band residual of the
+// plane-invariant levels from the same staging.
 //
-// Replaces, for the top level of the shared-stencil problems, the eight
-// colour launches of smooth.cu (region::gauss_seidel, region.cc:1557-1762,
+// Replaces, on those levels, the eight colour launches of smooth.cu
+// (region::gauss_seidel, region.cc:1557-1762,
 // in the 8-colour order q = (i&1) + 2(j&1) + 4(k&1)).  Colours 0-3 live on
 // even z-planes and 4-7 on odd ones, and a colour couples only to its own
 // plane and the planes above and below.  So a sweep is two launches (even
