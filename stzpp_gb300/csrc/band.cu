@@ -838,11 +838,14 @@ bool launch_band_kn(const LevelOp<T> &op, const Geom &g, const T *r, const T *xi
 // Threads per column of the sweep: in FP32 two on wide levels (64 or 128
 // sub-grid columns; four, with twice the warps, measured no faster: 350 vs
 // 347 us for two fine sweeps with 8-row bands, 131 vs 126 us on level 1,
-// where a thread's rows share each coefficient load) and four on narrow
-// ones (few nodes per row); one or two in FP64 (registers).
+// where a thread's rows share each coefficient load) and eight on narrow
+// ones, one row per thread: those levels have few CTAs and are bound by the
+// latency of each thread's chain (mixed solve 21.99 -> 21.65 ms against four
+// on the 16- and 8-column levels, 21.73 -> 21.68 ms on the 32-column one);
+// one or two in FP64 (registers).
 template <typename T, int M2, int KIND, bool SPARSE>
 bool launch_band_k(const LevelOp<T> &op, const Geom &g, const T *r, const T *xin, T *xout, cudaStream_t st) {
-    constexpr int NH = sizeof(T) == 4 ? (M2 >= 64 ? 2 : 4) : (M2 >= 64 ? 1 : 2);
+    constexpr int NH = sizeof(T) == 4 ? (M2 >= 64 ? 2 : 8) : (M2 >= 64 ? 1 : 2);
     return launch_band_kn<T, M2, NH, KIND, SPARSE>(op, g, r, xin, xout, st);
 }
 
