@@ -804,8 +804,8 @@ bool first_band_use(unsigned long long &devices) {
 }
 
 // Threads per column of the residual kernel: two (each thread two of the
-// band's four sub-rows; with one row, or four, the plane-invariant row's
-// products take more registers than a thread has).
+// band's four sub-rows, which share each coefficient load; four threads with
+// one row each measured slower: level 1 59.5 against 43.9 us).
 template <typename T, int M2>
 constexpr int kResNH = 2;
 
