@@ -8,7 +8,9 @@ residual (tests/test_gpu_parity.py::test_double_float_residual_matches_fp64).
     remainder, from the bits of x: |hi + lo - x| <= 2^-48 |x|;
   * a row b - sum a_t x_t with exact products (Dekker) and a two-sum high
     part (Knuth): error <= 2^-42 of sum |a_t x_t|, so residuals ten digits
-    below the terms keep their leading digits."""
+    below the terms keep their leading digits;
+  * the paired form of a symmetric row (opposite neighbours summed as a
+    double-float pair, one product per pair): the same bound."""
 from fractions import Fraction
 
 import numpy as np
@@ -87,6 +89,50 @@ def test_row_error_bound_with_cancellation():
         err = abs(Fraction(float(r)) - r_exact) / mag
         worst = max(worst, float(err))
         # the leading digits of a residual 1e-12 below the terms survive
+        if abs(r_exact) > Fraction(1, 10**12) * mag / 4:
+            assert abs(Fraction(float(r)) - r_exact) <= abs(r_exact) / 4
+    assert worst <= 2.0 ** -42, worst
+
+
+def add_pair(xh1, xl1, xh2, xl2):
+    """df_add: (xh1 + xl1) + (xh2 + xl2) with the high parts' sum exact
+    (Knuth's two-sum) and every rounding error in the float low part."""
+    s = F32(xh1 + xh2)
+    bv = F32(s - xh1)
+    err = F32(F32(xh1 - F32(s - bv)) + F32(xh2 - bv))
+    return s, F32(F32(xl1 + xl2) + err)
+
+
+def test_paired_row_error_bound_with_cancellation():
+    """The paired form of a symmetric row: the two opposite neighbours of
+    each coefficient summed as a double-float pair first, then one product
+    per pair.  Its error stays within 2^-42 of the row's sum |a x| (over the
+    unpaired terms), as the unpaired form's does, so residuals ten digits
+    below the terms keep their leading digits."""
+    rng = np.random.default_rng(2)
+    worst = 0.0
+    for _ in range(300):
+        npair = 21
+        a = rng.standard_normal(npair) * 65536.0
+        x1 = rng.standard_normal(npair) * 1e-3
+        x2 = rng.standard_normal(npair) * 1e-3
+        exact_sum = sum(Fraction(float(ai)) * (Fraction(float(u)) + Fraction(float(v)))
+                        for ai, u, v in zip(a, x1, x2))
+        mag = sum(abs(Fraction(float(ai)) * Fraction(float(u))) + abs(Fraction(float(ai)) * Fraction(float(v)))
+                  for ai, u, v in zip(a, x1, x2))
+        b = float(exact_sum + Fraction(float(rng.standard_normal() * 1e-12)) * mag)
+        r_exact = Fraction(b) - exact_sum
+        sh, sl = split([b])
+        sh, sl = sh[0], sl[0]
+        ah, al = split(a)
+        h1, l1 = split(x1)
+        h2, l2 = split(x2)
+        for t in range(npair):
+            ph, pl = add_pair(h1[t], l1[t], h2[t], l2[t])
+            sh, sl = sub_prod(sh, sl, ah[t], al[t], ph, pl)
+        r = F32(sh + sl)
+        err = abs(Fraction(float(r)) - r_exact) / mag
+        worst = max(worst, float(err))
         if abs(r_exact) > Fraction(1, 10**12) * mag / 4:
             assert abs(Fraction(float(r)) - r_exact) <= abs(r_exact) / 4
     assert worst <= 2.0 ** -42, worst
